@@ -1,0 +1,424 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 MLS-MPM engine: particle-substeps/s.
+
+A "step" is one MLS-MPM substep (binning, P2G, grid update, G2P) over the
+whole particle set of the workload.  Default workload: the large sparse
+scene, 16M particles in 64 ellipsoids on a 256^3 grid (elastic/snow, ground
+collider), seeded synthetic inputs.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                  [--workload ellipsoids_256|four_materials_128|water_cube_64]
+
+Prints one JSON line.  `value` times K substeps with state resident in HBM
+(CUDA events on the launching stream, barrier + synchronize on both sides,
+max over ranks).  `e2e` runs the drop-in API end to end: read_restart from
+pinned host arrays, step(frame_dt) frames and particle_info() readback.
+`--impl reference` times the CPU restatement of the reference's substep
+(C/OpenMP float32 oracle, all host threads) on a bounded sample.
+Under torchrun each rank runs an independent replica (replicas only: the
+single-scene substep has no data-parallel split without a halo exchange).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+ALGO_BYTES_PER_PARTICLE = 204  # read x,v,C,F,Jp,mat once (104) + write x,v,C,F,Jp (100)
+ALGO_BYTES_PER_NODE = 64  # P2G flush 16 + grid read 16 + grid write 16 + G2P read 16
+P2G_BYTES_PER_PARTICLE = 144  # read 104 + write F, Jp 40
+P2G_BYTES_PER_NODE = 16
+G2P_BYTES_PER_PARTICLE = 60  # write x, v, C
+G2P_BYTES_PER_NODE = 16
+GRID_BYTES_PER_NODE = 32
+KERNELS_PER_SUBSTEP = 9  # 6 binning kernels + p2g + grid + g2p
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def make_scene(name):
+    from taichi_elements_gb300 import scenes
+    return {
+        "ellipsoids_256": scenes.ellipsoids_256,
+        "four_materials_128": scenes.four_materials_128,
+        "water_cube_64": scenes.water_cube_64,
+    }[name]()
+
+
+def describe(sc):
+    return {
+        "ellipsoids_256": "3-D large sparse: 16M particles in 64 ellipsoids, 256^3 grid, elastic/snow 50/50, "
+                          "ground collider, f32",
+        "four_materials_128": "3-D multi-material: 4 cubes x 500K (water/elastic/snow/sand), 128^3 grid, f32",
+        "water_cube_64": "plain 3-D: water cube 134,218 particles, 64^3 grid, f32",
+    }[sc.name]
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.out = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is None:
+            return
+        time.sleep(0.15)
+        self.proc.terminate()
+        try:
+            self.out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            self.out = ""
+
+    def summary(self):
+        if not self.out:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_init():
+    import torch
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def count_nodes(solver):
+    """Distinct grid nodes touched by particle stencils (mass > 0)."""
+    import torch
+    v = solver.views()
+    ng = int(v["counters"][1].item())
+    gb = v["gblocks"][:ng].long()
+    addr = (gb[:, None] * 64 + torch.arange(64, device=gb.device)[None]).reshape(-1)
+    return int((v["grid_vel"][addr, 3] > 0).sum().item())
+
+
+def run_gb300(args):
+    import torch
+
+    from taichi_elements_gb300 import _lib
+    from taichi_elements_gb300.mpm_solver import MPMSolver
+
+    ws, rank, local = dist_init()
+    sc = make_scene(args.workload)
+    solver = sc.make_solver(chunk=args.chunk) if args.chunk else sc.make_solver()
+    dt = sc.default_dt
+    lib = solver._lib
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+
+    def substep_phases(ev=None):
+        p = solver.params
+        pp = ctypes.byref(p)
+        wsp, cap, n = solver._ws.data_ptr(), solver._cap, solver.n_particles
+        cur = solver._state[solver._cur].data_ptr()
+        nxt = solver._state[1 - solver._cur].data_ptr()
+        if ev is not None:
+            ev[0].record(stream)
+        _lib.check(lib.mpm_bin_finalize(pp, wsp, cap, n, sptr), "bin")
+        if ev is not None:
+            ev[1].record(stream)
+        _lib.check(lib.mpm_p2g(pp, wsp, cap, n, cur, nxt, dt, sptr), "p2g")
+        if ev is not None:
+            ev[2].record(stream)
+        _lib.check(lib.mpm_grid_update(pp, wsp, cap, dt, sptr), "grid")
+        if ev is not None:
+            ev[3].record(stream)
+        _lib.check(lib.mpm_g2p(pp, wsp, cap, n, nxt, dt, None, sptr), "g2p")
+        if ev is not None:
+            ev[4].record(stream)
+        solver._cur = 1 - solver._cur
+
+    solver._prepare(dt * (args.steps + args.warmup))
+    for _ in range(args.warmup):
+        substep_phases()
+    torch.cuda.synchronize()
+    n_nodes = count_nodes(solver)
+
+    # timed region: K substeps, per-phase CUDA events on the launching stream
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(5)] for _ in range(args.steps)]
+    start = torch.cuda.Event(enable_timing=True)
+    stop = torch.cuda.Event(enable_timing=True)
+    barrier(ws)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        start.record(stream)
+        for k in range(args.steps):
+            substep_phases(evs[k])
+        stop.record(stream)
+        torch.cuda.synchronize()
+    barrier(ws)
+    total_ms = allmax(start.elapsed_time(stop), ws)
+    st = int(solver._status.item())
+    if st:
+        raise RuntimeError(f"device status {st} during the benchmark")
+    ph = np.array([[e[i].elapsed_time(e[i + 1]) for i in range(4)] for e in evs])
+    ph_mean = ph.mean(0)
+    n = solver.n_particles
+    value = n * args.steps * ws / (total_ms / 1e3)
+    peak, peak_kind = load_peaks()
+    p2g_bytes = P2G_BYTES_PER_PARTICLE * n + P2G_BYTES_PER_NODE * n_nodes
+    p2g_ach = p2g_bytes / (ph_mean[1] / 1e3) / 1e9
+    sub_bytes = ALGO_BYTES_PER_PARTICLE * n + ALGO_BYTES_PER_NODE * n_nodes
+    sub_ach = sub_bytes / ((ph_mean[1] + ph_mean[2] + ph_mean[3]) / 1e3) / 1e9
+    full_ach = sub_bytes / (ph.sum(1).mean() / 1e3) / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        with open(tp) as f:
+            tj = json.load(f)
+        t = tj.get(args.workload, {}).get("p2g_dram_bytes_per_launch")
+        traffic = t
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(sc, args, ws)
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(sc, args)
+    line = {
+        "metric": "particle-substeps/s",
+        "value": value,
+        "unit": "particle-substeps/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded numpy scene generator; no dataset)",
+        "config": {
+            "workload": f"{sc.name}: {describe(sc)}",
+            "particles": n,
+            "grid": list(sc.res),
+            "grid_nodes_touched": n_nodes,
+            "dt": dt,
+            "l2": f"inputs larger than L2: particle state {n * 212 / 1e9:.2f} GB per buffer pair",
+            "parallelism": f"replicas x{ws}",
+            "chunk": solver.chunk,
+        },
+        "phases_ms": {"binning": ph_mean[0], "p2g": ph_mean[1], "grid": ph_mean[2], "g2p": ph_mean[3]},
+        "roofline": {"bound": "hbm", "kernel": "k_p2g", "achieved": p2g_ach, "peak": peak, "unit": "GB/s",
+                     "frac": p2g_ach / peak, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": p2g_bytes, "peak_source": peak_kind},
+        "roofline_substep": {"bound": "hbm", "kernels": "p2g+grid+g2p", "achieved": sub_ach, "peak": peak,
+                             "unit": "GB/s", "frac": sub_ach / peak,
+                             "with_binning": {"achieved": full_ach, "frac": full_ach / peak},
+                             "algorithmic_bytes_per_substep": sub_bytes, "peak_source": peak_kind},
+        "gpu_launches": KERNELS_PER_SUBSTEP * args.steps,
+        "clocks": clk.summary(),
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def run_e2e(sc, args, ws):
+    """End to end through the drop-in API: pinned host arrays -> read_restart
+    -> step(frame_dt) frames -> particle_info()."""
+    import torch
+
+    from taichi_elements_gb300.mpm_solver import MPMSolver
+    x = torch.from_numpy(sc.x).pin_memory()
+    v = torch.from_numpy(sc.v).pin_memory()
+    m = torch.from_numpy(sc.material).pin_memory()
+    c = torch.from_numpy(np.full(sc.n, 0xFFFFFF, np.int32)).pin_memory()
+    frames = args.e2e_frames
+    frame_dt = args.e2e_substeps * sc.default_dt * 0.999
+    count, _ = MPMSolver.count_substeps(frame_dt, sc.default_dt)
+
+    def once(timed):
+        s = MPMSolver(sc.res, size=sc.size)
+        for cc in sc.postprocess:
+            s.add_surface_collider(cc["point"], cc["normal"], cc.get("surface", 0), cc.get("friction", 0.0))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.read_restart(sc.n, x.numpy(), v.numpy(), m.numpy(), c.numpy())
+        outs = []
+        for _ in range(frames):
+            s.step(frame_dt)
+            outs.append(s.particle_info())
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0
+
+    once(False)  # warm-up: library, allocations, CUDA-graph capture
+    barrier(ws)
+    t = allmax(once(True), ws)
+    h2d = sc.n * (12 + 12 + 4 + 4)
+    d2h = sc.n * (12 + 12 + 4 + 4)
+    return {"value": sc.n * count * frames * ws / t, "unit": "particle-substeps/s",
+            "h2d_bytes_per_step": h2d / frames, "d2h_bytes_per_step": d2h,
+            "step": f"one step(frame_dt) frame of {count} substeps + particle_info(); read_restart of the scene "
+                    f"from pinned host memory inside the timed region (amortised over {frames} frames)",
+            "frames": frames, "seconds": t}
+
+
+def cpu_baseline(sc, args, budget_s=None):
+    """The oracle port (C/OpenMP float32, every host thread) on a bounded
+    sample: whole-scene substeps until the time budget is used."""
+    from oracle import oracle as O
+    budget_s = budget_s or args.cpu_budget
+    cfg = O.Config(res=sc.res, size=sc.size, postprocess=[dict(kind=O.KIND_BOX, surface=0)] + list(sc.postprocess))
+    P = O.Particles.seeded(sc.x, sc.material, v=sc.v, dtype=np.float32)
+    threads = os.cpu_count() or 1
+    R = O.Runner(cfg, P, nthreads=threads)
+    dt = sc.default_dt
+    R.run(dt, 1)  # warm-up (page-in)
+    done = 0
+    t0 = time.perf_counter()
+    while True:
+        R.run(dt, 1)
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    el = time.perf_counter() - t0
+    return {"value": sc.n * done / el, "unit": "particle-substeps/s", "cores": threads, "kind": "port",
+            "sample": f"{done} substeps of the full {sc.n}-particle scene ({el:.1f} s)"}
+
+
+def run_reference(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    sc = make_scene(args.workload)
+    cfg = O.Config(res=sc.res, size=sc.size, postprocess=[dict(kind=O.KIND_BOX, surface=0)] + list(sc.postprocess))
+    P = O.Particles.seeded(sc.x, sc.material, v=sc.v, dtype=np.float32)
+    threads = os.cpu_count() or 1
+    R = O.Runner(cfg, P, nthreads=threads)
+    dt = sc.default_dt
+    for _ in range(args.warmup):
+        R.run(dt, 1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        R.run(dt, 1)
+    el = time.perf_counter() - t0
+    value = sc.n * args.steps / el
+    line = {
+        "impl": "reference",
+        "metric": "particle-substeps/s",
+        "value": value,
+        "unit": "particle-substeps/s",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": el / args.steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded numpy scene generator; no dataset)",
+        "config": {"workload": f"{sc.name}: {describe(sc)}", "particles": sc.n, "grid": list(sc.res),
+                   "parallelism": "host CPU"},
+        "cpu_baseline": {"value": value, "unit": "particle-substeps/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} whole-scene substeps after {args.warmup} warm-up substeps; "
+                                   "the reference's Taichi runtime is not installable here, so its substep "
+                                   "runs as the C/OpenMP restatement"},
+        "e2e": {"value": value, "unit": "particle-substeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=None)
+    ap.add_argument("--warmup", type=int, default=None)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="ellipsoids_256",
+                    choices=["ellipsoids_256", "four_materials_128", "water_cube_64"])
+    ap.add_argument("--chunk", type=int, default=None)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--e2e-frames", type=int, default=3)
+    ap.add_argument("--e2e-substeps", type=int, default=50)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        args.steps = 3 if args.steps is None else args.steps
+        args.warmup = 1 if args.warmup is None else args.warmup
+        run_reference(args)
+    else:
+        args.steps = 200 if args.steps is None else args.steps
+        args.warmup = 5 if args.warmup is None else args.warmup
+        if args.warmup < 3:
+            args.warmup = 3
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

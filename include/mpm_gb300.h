@@ -1,0 +1,171 @@
+/*
+ * mpm_gb300.h - C ABI of the GB300-native MLS-MPM engine (libmpm_gb300.so).
+ *
+ * The reference (taichi-dev/taichi_elements) has no FFI: its operator API is
+ * the Python class engine.mpm_solver.MPMSolver, whose @ti.kernel methods are
+ * the hot path.  Each entry point below replaces one of those kernels (or a
+ * piece of the Taichi runtime they rely on) and is called through ctypes by
+ * taichi_elements_gb300/mpm_solver.py, the drop-in MPMSolver.
+ *
+ * Conventions
+ *  - Every entry point returns 0 on success or a negative MPM_E_* code; it
+ *    never allocates device memory.  All buffers are owned by the caller.
+ *  - Pointers are device pointers unless named host_*; `stream` is a
+ *    cudaStream_t passed as void*.  Launches are asynchronous.
+ *  - Device-side faults (positions outside the grid window, NaN/Inf, table
+ *    overflow) are reported through the status word of the workspace
+ *    (MPM_STATUS_* bits), never by trapping.
+ *
+ * Particle state ("pstate") is one float32 buffer of MPM_NROWS rows of `cap`
+ * elements (structure of arrays, row r starts at pstate + r*cap):
+ *   rows 0-2 x, 3-5 v, 6-14 C (row-major 3x3), 15-23 F (row-major 3x3),
+ *   24 Jp, 25 material (int32 bits), 26 original particle id (int32 bits),
+ *   27 per-particle Young's modulus (used only when MpmParams.has_Ep != 0).
+ * The engine ping-pongs between two such buffers: a substep reads buffer
+ * `cur` in any order and writes buffer `nxt` sorted by grid block.
+ */
+#ifndef MPM_GB300_H
+#define MPM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MPM_ABI_VERSION 1
+#define MPM_NROWS 28
+#define MPM_MAX_COLLIDERS 16 /* post-process records, box included */
+
+/* status bits (workspace status word) */
+#define MPM_STATUS_OUT_OF_GRID 1u  /* a stencil left the grid window (clamped) */
+#define MPM_STATUS_NONFINITE 2u    /* NaN/Inf particle position */
+#define MPM_STATUS_TABLE_OVERFLOW 4u
+
+/* error codes */
+#define MPM_OK 0
+#define MPM_E_INVALID (-1)
+#define MPM_E_CUDA (-2)
+#define MPM_E_VERSION (-3)
+#define MPM_E_CAPACITY (-4)
+
+/* Grid post-process record, applied in list order after gravity, as the
+ * reference's grid_postprocess list (engine/mpm_solver.py:300-302, 794-795).
+ * kind 0 = surface (half-space) collider, engine/mpm_solver.py:647-687
+ * (add_surface_collider); kind 1 = sphere, :618-642 (add_sphere_collider);
+ * kind 2 = bounding box, :600-616 and :689-692 (add_bounding_box), whose
+ * `surface` field holds the `unbounded` flag.  surface: 0 sticky, 1 slip,
+ * 2 separate (engine/mpm_solver.py:29-42). */
+typedef struct MpmCollider {
+  int32_t kind;
+  int32_t surface;
+  float point[3];  /* plane point / sphere centre */
+  float normal[3]; /* unit normal (plane) */
+  float radius;    /* sphere radius */
+  float friction;  /* plane friction */
+} MpmCollider;
+
+/* Solver constants, engine/mpm_solver.py:44-310.  All float fields are the
+ * float32 values of the reference's Python-double constants. */
+typedef struct MpmParams {
+  int32_t version; /* MPM_ABI_VERSION */
+  int32_t res[3];
+  int32_t padding;
+  int32_t unbounded;
+  int32_t grid_size; /* reference grid_size (4096, grown when unbounded) */
+  int32_t n_colliders;
+  int32_t win_lo[3]; /* grid window origin, node index, multiple of 4 */
+  int32_t win_nb[3]; /* grid window extent in 4^3 blocks */
+  int32_t has_Ep;    /* per-particle Young's modulus in pstate row 27 */
+  int32_t chunk;     /* particles per P2G/G2P work item (multiple of 32) */
+  float dx, inv_dx, p_vol, p_mass;
+  float mu0, la0, nu, alpha; /* Lame parameters, Poisson ratio, sand alpha */
+  float water_density;
+  float gravity[3];
+  float stress_k; /* p_vol * 4 * inv_dx^2            (mpm_solver.py:569) */
+  float sand_k;   /* (3 la0 + 2 mu0) / (2 mu0)        (mpm_solver.py:335-337) */
+  MpmCollider colliders[MPM_MAX_COLLIDERS];
+} MpmParams;
+
+/* Library ABI version (MPM_ABI_VERSION). */
+int mpm_abi_version(void);
+
+/* Bytes of scratch (workspace) a solver with this grid window and particle
+ * capacity needs.  Replaces the Taichi SNode tree of
+ * engine/mpm_solver.py:161-196 (pointer/dense grid and per-block pid lists)
+ * and the particle dynamic SNode chunking of :212-214. */
+int mpm_workspace_bytes(const MpmParams *p, int64_t cap, size_t *bytes_out);
+
+/* Zero the persistent parts of a fresh workspace (cell counters, block
+ * flags, grids, status).  Call once after allocating it. */
+int mpm_workspace_init(const MpmParams *p, void *ws, int64_t cap, void *stream);
+
+/* Bin particles [begin, end) of `pstate` into the grid: per-particle cell key
+ * and rank within the cell.  Replaces build_pid, engine/mpm_solver.py:344-361
+ * (the substep engine does this for the next substep inside mpm_g2p; this
+ * entry point bins freshly seeded particles, engine/mpm_solver.py:840-850,
+ * 969-978, 1081-1144). */
+int mpm_bin_count(const MpmParams *p, void *ws, int64_t cap, const float *pstate, int64_t begin,
+                  int64_t end, void *stream);
+
+/* Turn the counts into the active-block list, the dilated grid-block list,
+ * per-block particle ranges and the sorted particle order (`pid`).  Second
+ * half of build_pid (engine/mpm_solver.py:344-361) plus the sparse grid
+ * activation of grid.deactivate_all()/P2G writes (:789, :582-584). */
+int mpm_bin_finalize(const MpmParams *p, void *ws, int64_t cap, int64_t n, void *stream);
+
+/* P2G: engine/mpm_solver.py:487-584 (with sand_projection :321-342).  Reads
+ * `cur` through the sorted order, writes the updated F/Jp and the carried
+ * particle fields into `nxt` in sorted order, and scatters mass and momentum
+ * into the grid. */
+int mpm_p2g(const MpmParams *p, void *ws, int64_t cap, int64_t n, const float *cur, float *nxt,
+            float dt, void *stream);
+
+/* Grid update: engine/mpm_solver.py:586-616 (momentum to velocity, gravity,
+ * bounding box) and :618-687 (colliders in insertion order), fused, over the
+ * active grid blocks only. Also clears the momentum grid for the next P2G. */
+int mpm_grid_update(const MpmParams *p, void *ws, int64_t cap, float dt, void *stream);
+
+/* G2P: engine/mpm_solver.py:694-724, in place on `nxt`, fused with the next
+ * substep's binning (build_pid, :344-361) and the max-|v| reduction
+ * (compute_max_velocity, :726-735) into `maxv_out` (may be NULL). */
+int mpm_g2p(const MpmParams *p, void *ws, int64_t cap, int64_t n, float *nxt, float dt,
+            float *maxv_out, void *stream);
+
+/* One substep = finalize + p2g + grid update + g2p; engine/mpm_solver.py:789-799.
+ * After it returns (on the stream), `nxt` holds the state. */
+int mpm_substep(const MpmParams *p, void *ws, int64_t cap, int64_t n, const float *cur, float *nxt,
+                float dt, float *maxv_out, void *stream);
+
+/* Copy rows of the sorted state back to original particle order:
+ * out[id[j]*ncols + c] = pstate[(row0 + c)*cap + j] for c < ncols.
+ * Replaces copy_dynamic_nd / copy_dynamic, engine/mpm_solver.py:1146-1191. */
+int mpm_gather_rows(const float *pstate, int64_t cap, int64_t n, int32_t row0, int32_t ncols,
+                    float *out, void *stream);
+
+/* Pointer to the device status word inside the workspace (uint32). */
+int mpm_status_ptr(const MpmParams *p, void *ws, int64_t cap, uint32_t **status_out);
+
+/* Diagnostics views inside the workspace (device pointers), used by the
+ * parity tests: counters (int32[16]: 0 #particle blocks, 1 #grid blocks,
+ * 2 #work items, 3 status, 4 #particles binned), the particle-block list,
+ * the grid-block list, per-particle-block counts and starts, and the sorted
+ * order. */
+typedef struct MpmViews {
+  int32_t *counters;
+  int32_t *pblocks;
+  int32_t *gblocks;
+  int32_t *pblock_count;
+  int32_t *pblock_start;
+  int32_t *pid;
+  int32_t *cellkey;
+  float *grid_mom; /* float4 per node (m, mv) in window block-major order */
+  float *grid_vel; /* float4 per node (v, m) */
+} MpmViews;
+int mpm_views(const MpmParams *p, void *ws, int64_t cap, MpmViews *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

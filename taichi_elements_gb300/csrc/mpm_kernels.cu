@@ -1,0 +1,773 @@
+// GB300 (sm_103a) kernels of the MLS-MPM substep and their C ABI.
+//
+// Pipeline of one substep (engine/mpm_solver.py:789-799 of
+// taichi-dev/taichi_elements), all on one stream, no host synchronisation:
+//
+//   k_flags_count/k_flags_write   active 4^3 blocks -> ordered compact lists
+//                                 (particle blocks, and grid blocks = particle
+//                                 blocks dilated by {0,1}^3)
+//   k_pb_stats/k_pb_scan          per particle block: count, start, level
+//                                 table base and work-item base (two-pass scan)
+//   k_pb_levels                   rank-major level tables, work items, clears
+//                                 the cell counters and block flags
+//   k_scatter                     sorted order pid[pos] = i
+//   k_p2g                         per work item: stress, APIC scatter into a
+//                                 shared-memory 6^3 tile, one float4 atomic
+//                                 flush per touched node
+//   k_grid                        momentum->velocity, gravity, box, colliders
+//   k_g2p                         per work item: 6^3 velocity tile in shared
+//                                 memory, gather, advect, bin for next substep
+//
+// Sorted order inside a block is rank-major: all cells' first particles (in
+// cell order), then all cells' second particles, ...  Consecutive lanes thus
+// work on different cells, so their shared-memory atomics and gathers hit
+// different nodes, while global loads stay coalesced.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <mutex>
+
+#include "mpm_common.cuh"
+
+namespace mpm {
+
+constexpr int kP2GThreads = 128;
+constexpr int kG2PThreads = 128;
+
+__device__ __forceinline__ void set_status(const Ws &w, uint32_t bits) {
+  if (bits) atomicOr((unsigned int *)&w.counters[3], bits);
+}
+
+// ------------------------------------------------------------ binning ----
+
+// kNeighbourMask[need]: bits of all neighbour offsets d (dx*4+dy*2+dz) whose
+// set bits are a subset of `need`.
+__constant__ int kNeighbourMask[8] = {0x01, 0x03, 0x05, 0x0F, 0x11, 0x33, 0x55, 0xFF};
+
+__device__ __forceinline__ void bin_one(const MpmParams &P, const Ws &w, int64_t i, float x0, float x1,
+                                        float x2, uint32_t &bad) {
+  const Base b = particle_base(P, x0, x1, x2, bad);
+  const int key = cell_key(P, b);
+  const int r = atomicAdd(&w.cell_cnt[key], 1);
+  const int blin = key >> 6;
+  // Blocks this particle's 3^3 stencil reaches: its own block plus, per axis,
+  // the next block when the base sits in the last two cells of the block.
+  // Bit (dx*4 + dy*2 + dz) of the flag marks block b + (dx,dy,dz); the
+  // grid-active set is then exactly the set of blocks holding stencil nodes
+  // (the blocks the reference's sparse grid activates in P2G, :582-584).
+  const int need = ((b.b[0] & 3) >= 2 ? 4 : 0) | ((b.b[1] & 3) >= 2 ? 2 : 0) | ((b.b[2] & 3) >= 2 ? 1 : 0);
+  const int mask = kNeighbourMask[need];
+  if ((w.blk_flag[blin] & mask) != mask) atomicOr(&w.blk_flag[blin], mask);
+  w.cellkey[i] = key;
+  w.rank[i] = r;
+}
+
+__global__ void k_bin_count(const MpmParams P, const Ws w, const float *__restrict__ ps, int64_t cap,
+                            int64_t begin, int64_t end) {
+  const int64_t i = begin + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t bad = 0;
+  if (i < end) bin_one(P, w, i, ps[kX * cap + i], ps[(kX + 1) * cap + i], ps[(kX + 2) * cap + i], bad);
+  set_status(w, bad);
+}
+
+__device__ __forceinline__ void block_coords(const MpmParams &P, int64_t b, int &bx, int &by, int &bz) {
+  bz = (int)(b % P.win_nb[2]);
+  by = (int)((b / P.win_nb[2]) % P.win_nb[1]);
+  bx = (int)(b / ((int64_t)P.win_nb[1] * P.win_nb[2]));
+}
+
+// grid-active = some particle block b - d whose stencils reach b (bit d)
+__device__ __forceinline__ bool grid_flag(const MpmParams &P, const Ws &w, int64_t b) {
+  int bx, by, bz;
+  block_coords(P, b, bx, by, bz);
+  const int64_t sy = P.win_nb[2], sx = (int64_t)P.win_nb[1] * P.win_nb[2];
+  bool f = false;
+#pragma unroll
+  for (int dx = 0; dx < 2; ++dx)
+#pragma unroll
+    for (int dy = 0; dy < 2; ++dy)
+#pragma unroll
+      for (int dz = 0; dz < 2; ++dz)
+        if (bx >= dx && by >= dy && bz >= dz)
+          f |= ((w.blk_flag[b - dx * sx - dy * sy - dz] >> (dx * 4 + dy * 2 + dz)) & 1) != 0;
+  return f;
+}
+
+template <typename T>
+__device__ __forceinline__ T block_sum_256(T v, T *sh) {
+  // inclusive-sum of a 256-thread CTA; returns the total; sh needs 8 slots
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  T t = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) t += sh[k];
+  __syncthreads();
+  return t;
+}
+
+// exclusive scan across a 256-thread CTA; returns the exclusive prefix and
+// writes the CTA total to *total.  sh needs 8 slots.
+__device__ __forceinline__ int block_excl_scan_256(int v, int *sh, int *total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int n = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += n;
+  }
+  if (lane == 31) sh[wid] = inc;
+  __syncthreads();
+  int before = 0, tot = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const int s = sh[k];
+    before += (k < wid) ? s : 0;
+    tot += s;
+  }
+  __syncthreads();
+  *total = tot;
+  return before + inc - v;
+}
+
+__global__ __launch_bounds__(256) void k_flags_count(const MpmParams P, const Ws w) {
+  __shared__ int sh[8];
+  int cp = 0, cg = 0;
+  for (int q = 0; q < kFlagTile / 256; ++q) {
+    const int64_t b = (int64_t)blockIdx.x * kFlagTile + q * 256 + threadIdx.x;
+    if (b < w.nblk) {
+      cp += w.blk_flag[b] != 0;
+      cg += grid_flag(P, w, b);
+    }
+  }
+  const int tp = block_sum_256(cp, sh);
+  const int tg = block_sum_256(cg, sh);
+  if (threadIdx.x == 0) {
+    w.flag_tiles[2 * blockIdx.x] = tp;
+    w.flag_tiles[2 * blockIdx.x + 1] = tg;
+  }
+}
+
+__global__ __launch_bounds__(256) void k_flags_write(const MpmParams P, const Ws w) {
+  __shared__ int sh[8];
+  // offsets of this tile = sum over preceding tiles
+  int op = 0, og = 0;
+  for (int t = threadIdx.x; t < (int)blockIdx.x; t += 256) {
+    op += w.flag_tiles[2 * t];
+    og += w.flag_tiles[2 * t + 1];
+  }
+  op = block_sum_256(op, sh);
+  og = block_sum_256(og, sh);
+  for (int q = 0; q < kFlagTile / 256; ++q) {
+    const int64_t b = (int64_t)blockIdx.x * kFlagTile + q * 256 + threadIdx.x;
+    int fp = 0, fg = 0;
+    if (b < w.nblk) {
+      fp = w.blk_flag[b] != 0;
+      fg = grid_flag(P, w, b);
+    }
+    int totp, totg;
+    const int ep = block_excl_scan_256(fp, sh, &totp);
+    const int eg = block_excl_scan_256(fg, sh, &totg);
+    if (fp) {
+      w.pblocks[op + ep] = (int)b;
+      w.blk_slot[b] = op + ep;
+    }
+    if (fg) w.gblocks[og + eg] = (int)b;
+    op += totp;
+    og += totg;
+  }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
+    w.counters[0] = op;
+    w.counters[1] = og;
+    w.counters[2] = 0;
+    w.counters[4] = 0;
+  }
+}
+
+__global__ __launch_bounds__(256) void k_pb_stats(const MpmParams P, const Ws w) {
+  __shared__ int sh[8];
+  const int npb = w.counters[0];
+  if ((int64_t)blockIdx.x * kStatTile >= npb) return;
+  const int k = blockIdx.x * kStatTile + threadIdx.x;
+  int n = 0, mx = 0, ni = 0;
+  if (k < npb) {
+    const int4 *c4 = reinterpret_cast<const int4 *>(w.cell_cnt + (int64_t)w.pblocks[k] * kBlockCells);
+#pragma unroll 4
+    for (int q = 0; q < 16; ++q) {
+      const int4 c = c4[q];
+      n += c.x + c.y + c.z + c.w;
+      mx = max(mx, max(max(c.x, c.y), max(c.z, c.w)));
+    }
+    ni = (n + P.chunk - 1) / P.chunk;
+  }
+  int tn, tm, ti;
+  const int en = block_excl_scan_256(n, sh, &tn);
+  const int em = block_excl_scan_256(mx, sh, &tm);
+  const int ei = block_excl_scan_256(ni, sh, &ti);
+  if (k < npb) {
+    w.pb_count[k] = n;
+    w.pb_start[k] = en;
+    w.pb_lvl[k] = em;
+    w.pb_item[k] = ei;
+  }
+  if (threadIdx.x == 0) {
+    w.pb_tiles[3 * blockIdx.x] = tn;
+    w.pb_tiles[3 * blockIdx.x + 1] = tm;
+    w.pb_tiles[3 * blockIdx.x + 2] = ti;
+  }
+}
+
+__global__ __launch_bounds__(256) void k_pb_scan(const MpmParams P, const Ws w) {
+  __shared__ int sh[8];
+  const int npb = w.counters[0];
+  if ((int64_t)blockIdx.x * kStatTile >= npb) return;
+  int on = 0, om = 0, oi = 0;
+  for (int t = threadIdx.x; t < (int)blockIdx.x; t += 256) {
+    on += w.pb_tiles[3 * t];
+    om += w.pb_tiles[3 * t + 1];
+    oi += w.pb_tiles[3 * t + 2];
+  }
+  on = block_sum_256(on, sh);
+  om = block_sum_256(om, sh);
+  oi = block_sum_256(oi, sh);
+  const int k = blockIdx.x * kStatTile + threadIdx.x;
+  if (k < npb) {
+    const int s = w.pb_start[k] + on;
+    const int it = w.pb_item[k] + oi;
+    w.pb_start[k] = s;
+    w.pb_lvl[k] += om;
+    w.pb_item[k] = it;
+    if (k == npb - 1) {
+      const int c = w.pb_count[k];
+      w.counters[2] = it + (c + P.chunk - 1) / P.chunk;
+      w.counters[4] = s + c;
+    }
+  }
+}
+
+// One warp per particle block: rank-major level table, work items, and the
+// clearing of the cell counters and the block flag.
+__global__ __launch_bounds__(256) void k_pb_levels(const MpmParams P, const Ws w, int64_t cap) {
+  const int npb = w.counters[0];
+  const int lane = threadIdx.x & 31;
+  const int nwarps = gridDim.x * (blockDim.x >> 5);
+  for (int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < npb; k += nwarps) {
+    const int blin = w.pblocks[k];
+    int32_t *cc = w.cell_cnt + (int64_t)blin * kBlockCells;
+    const int c0 = cc[lane], c1 = cc[lane + 32];
+    int mx = max(c0, c1);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    const int lvl = w.pb_lvl[k];
+    if ((int64_t)lvl + mx > cap) {  // counts exceed the capacity: binning is stale
+      if (lane == 0) set_status(w, MPM_STATUS_TABLE_OVERFLOW);
+      mx = 0;
+    }
+    int L = 0;
+    for (int r = 0; r < mx; ++r) {
+      const unsigned m0 = __ballot_sync(0xffffffffu, c0 > r);
+      const unsigned m1 = __ballot_sync(0xffffffffu, c1 > r);
+      if (lane == 0) {
+        w.lvl_mask[lvl + r] = (unsigned long long)m0 | ((unsigned long long)m1 << 32);
+        w.lvl_L[lvl + r] = L;
+      }
+      L += __popc(m0) + __popc(m1);
+    }
+    const int n = w.pb_count[k], st = w.pb_start[k], ib = w.pb_item[k];
+    const int ni = (n + P.chunk - 1) / P.chunk;
+    for (int j = lane; j < ni; j += 32) {
+      if (ib + j < w.items_cap)
+        w.items[ib + j] = make_int2(k, st + j * P.chunk);
+      else
+        set_status(w, MPM_STATUS_TABLE_OVERFLOW);
+    }
+    cc[lane] = 0;
+    cc[lane + 32] = 0;
+    if (lane == 0) w.blk_flag[blin] = 0;
+  }
+}
+
+__global__ void k_scatter(const MpmParams P, const Ws w, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int key = w.cellkey[i];
+  const int r = w.rank[i];
+  const int blin = key >> 6, c = key & 63;
+  const int k = w.blk_slot[blin];
+  if (k < 0 || k >= w.counters[0] || r < 0) {  // stale binning: report, never index out of range
+    set_status(w, MPM_STATUS_TABLE_OVERFLOW);
+    return;
+  }
+  const int lv = w.pb_lvl[k] + r;
+  if (lv >= n) {
+    set_status(w, MPM_STATUS_TABLE_OVERFLOW);
+    return;
+  }
+  const unsigned long long below = c == 0 ? 0ull : (w.lvl_mask[lv] & ((1ull << c) - 1ull));
+  const int pos = w.pb_start[k] + w.lvl_L[lv] + __popcll(below);
+  if (pos < 0 || pos >= n) {
+    set_status(w, MPM_STATUS_TABLE_OVERFLOW);
+    return;
+  }
+  w.pid[pos] = (int)i;
+}
+
+// ---------------------------------------------------------------- P2G ----
+//
+// Each warp scatters into its own float4 tile (m, mv) of the block's 6^3
+// nodes with plain shared-memory read-modify-writes, one stencil offset at a
+// time with a __syncwarp() between offsets.  Within one offset step the lanes
+// touch distinct nodes as long as their cells differ, which the rank-major
+// particle order guarantees inside a level; the rare lanes that share a cell
+// (a warp straddling two short levels) are found with __match_any_sync and
+// scatter in later rounds.  No shared-memory float atomics are used.  At the
+// end of a work item the warps' tiles are summed and flushed to the grid with
+// one float4 global reduction per touched node.
+
+constexpr int kP2GWarps = kP2GThreads / 32;
+
+__device__ __forceinline__ float4 f4add(float4 a, float4 b) {
+  return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+}
+
+template <bool HAS_EP>
+__global__ __launch_bounds__(kP2GThreads, 5) void k_p2g(const MpmParams P, const Ws w,
+                                                       const float *__restrict__ cur,
+                                                       float *__restrict__ nxt, int64_t cap, float dt) {
+  __shared__ float4 tiles[kP2GWarps][kTileN];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float4 *tile = tiles[warp];
+  const int nitems = (int)min((int64_t)w.counters[2], w.items_cap);
+  uint32_t bad = 0;
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const int2 item = w.items[it];
+    const int k = item.x, start = item.y;
+    const int end = (int)min((int64_t)min(start + P.chunk, w.pb_start[k] + w.pb_count[k]), cap);
+    int bx, by, bz;
+    block_coords(P, w.pblocks[k], bx, by, bz);
+    for (int t = lane; t < kTileN; t += 32) tile[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncwarp();
+    for (int j0 = start + warp * 32; j0 < end; j0 += kP2GThreads) {
+      const int j = j0 + lane;
+      bool active = j < end;
+      int64_t i = active ? w.pid[j] : 0;
+      if (active && (i < 0 || i >= cap)) {
+        bad |= MPM_STATUS_TABLE_OVERFLOW;
+        active = false;
+      }
+      int cell = -1 - lane;  // unique per inactive lane
+      float mass = 0.f, q[3] = {0.f, 0.f, 0.f}, adx[3][3];
+      float wt[3][3];
+      int lx = 0, ly = 0, lz = 0;
+      if (active) {
+        float x[3], v[3], C[3][3], F[3][3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          x[d] = cur[(kX + d) * cap + i];
+          v[d] = cur[(kV + d) * cap + i];
+        }
+#pragma unroll
+        for (int a = 0; a < 9; ++a) {
+          C[a / 3][a % 3] = cur[(kC + a) * cap + i];
+          F[a / 3][a % 3] = cur[(kF + a) * cap + i];
+        }
+        float Jp = cur[kJp * cap + i];
+        const int mat = __float_as_int(cur[kMat * cap + i]);
+        const float idf = cur[kId * cap + i];
+        const float Ep = HAS_EP ? cur[kEp * cap + i] : 0.0f;
+        const Base b = particle_base(P, x[0], x[1], x[2], bad);
+        const P2GOut o = constitutive(P, dt, mat, Ep, F, Jp, C);
+        // carried fields, sorted position j
+#pragma unroll
+        for (int d = 0; d < 3; ++d) nxt[(kX + d) * cap + j] = x[d];
+#pragma unroll
+        for (int a = 0; a < 9; ++a) nxt[(kF + a) * cap + j] = F[a / 3][a % 3];
+        nxt[kJp * cap + j] = Jp;
+        nxt[kMat * cap + j] = __int_as_float(mat);
+        nxt[kId * cap + j] = idf;
+        if (HAS_EP) nxt[kEp * cap + j] = Ep;
+        if (mat == 4) {  // stationary: G2P keeps v and C (:722)
+#pragma unroll
+          for (int d = 0; d < 3; ++d) nxt[(kV + d) * cap + j] = v[d];
+#pragma unroll
+          for (int a = 0; a < 9; ++a) nxt[(kC + a) * cap + j] = C[a / 3][a % 3];
+        }
+        lx = b.b[0] - bx * 4;
+        ly = b.b[1] - by * 4;
+        lz = b.b[2] - bz * 4;
+        if ((unsigned)lx > 3u || (unsigned)ly > 3u || (unsigned)lz > 3u) {  // moved since binning
+          bad |= MPM_STATUS_TABLE_OVERFLOW;
+          active = false;
+        } else {
+          cell = (lx * 4 + ly) * 4 + lz;
+          bspline_weights(b.fx, wt);
+          mass = o.mass;
+          // APIC scatter, :576-584: node value = w * (m v + A (off - fx) dx)
+#pragma unroll
+          for (int d = 0; d < 3; ++d)
+            q[d] = o.mass * v[d] -
+                   P.dx * (o.affine[d][0] * b.fx[0] + o.affine[d][1] * b.fx[1] + o.affine[d][2] * b.fx[2]);
+#pragma unroll
+          for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) adx[r][c] = o.affine[r][c] * P.dx;
+        }
+      }
+      // lanes sharing a cell scatter in successive rounds
+      const unsigned peers = __match_any_sync(0xffffffffu, cell);
+      const int round_of_lane = __popc(peers & ((1u << lane) - 1u));
+      for (int round = 0;; ++round) {
+        const bool mine = active && round_of_lane == round;
+        const int base_node = (lx * kTileW + ly) * kTileW + lz;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int bb = 0; bb < 3; ++bb) {
+            const float wab = wt[a][0] * wt[bb][1];
+            float pab[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) pab[d] = q[d] + adx[d][0] * (float)a + adx[d][1] * (float)bb;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              if (mine) {
+                const float wgt = wab * wt[c][2];
+                float4 *nd = tile + base_node + (a * kTileW + bb) * kTileW + c;
+                float4 g = *nd;
+                g.x = fmaf(wgt, mass, g.x);
+                g.y = fmaf(wgt, pab[0] + adx[0][2] * (float)c, g.y);
+                g.z = fmaf(wgt, pab[1] + adx[1][2] * (float)c, g.z);
+                g.w = fmaf(wgt, pab[2] + adx[2][2] * (float)c, g.w);
+                *nd = g;
+              }
+              __syncwarp();
+            }
+          }
+        if (!__any_sync(0xffffffffu, active && round_of_lane > round)) break;
+      }
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < kTileN; t += blockDim.x) {
+      float4 g = tiles[0][t];
+#pragma unroll
+      for (int q = 1; q < kP2GWarps; ++q) g = f4add(g, tiles[q][t]);
+      if (g.x != 0.0f) {
+        const int tx = t / 36, ty = (t / 6) % 6, tz = t % 6;
+        const int gx = bx * 4 + tx, gy = by * 4 + ty, gz = bz * 4 + tz;
+        if (gx < P.win_nb[0] * 4 && gy < P.win_nb[1] * 4 && gz < P.win_nb[2] * 4)
+          atomicAdd(&w.grid_mom[node_addr(P, gx, gy, gz)], g);
+      }
+    }
+    __syncthreads();
+  }
+  set_status(w, bad);
+}
+
+// --------------------------------------------------------------- grid ----
+
+__global__ __launch_bounds__(256) void k_grid(const MpmParams P, const Ws w, float dt) {
+  const int ng = w.counters[1];
+  const int64_t total = (int64_t)ng * kBlockCells;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int blin = w.gblocks[t >> 6];
+    const int l = (int)(t & 63);
+    const int64_t addr = (int64_t)blin * kBlockCells + l;
+    const float4 g = w.grid_mom[addr];
+    w.grid_mom[addr] = make_float4(0.f, 0.f, 0.f, 0.f);
+    int bx, by, bz;
+    block_coords(P, blin, bx, by, bz);
+    const int I[3] = {P.win_lo[0] + bx * 4 + (l >> 4), P.win_lo[1] + by * 4 + ((l >> 2) & 3),
+                      P.win_lo[2] + bz * 4 + (l & 3)};
+    const float3 v = grid_node_update(P, I, g.x, make_float3(g.y, g.z, g.w), dt);
+    w.grid_vel[addr] = make_float4(v.x, v.y, v.z, g.x);
+  }
+}
+
+// ---------------------------------------------------------------- G2P ----
+
+__global__ __launch_bounds__(kG2PThreads, 8) void k_g2p(const MpmParams P, const Ws w, float *__restrict__ st,
+                                                       int64_t cap, float dt, float *maxv_out) {
+  __shared__ float4 vt[kTileN];
+  const int nitems = (int)min((int64_t)w.counters[2], w.items_cap);
+  uint32_t bad = 0;
+  float vmax = 0.0f;
+  const float s4 = 4.0f * P.inv_dx;
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const int2 item = w.items[it];
+    const int k = item.x, start = item.y;
+    const int end = (int)min((int64_t)min(start + P.chunk, w.pb_start[k] + w.pb_count[k]), cap);
+    int bx, by, bz;
+    block_coords(P, w.pblocks[k], bx, by, bz);
+    for (int t = threadIdx.x; t < kTileN; t += blockDim.x) {
+      const int tx = t / 36, ty = (t / 6) % 6, tz = t % 6;
+      const int gx = bx * 4 + tx, gy = by * 4 + ty, gz = bz * 4 + tz;
+      float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (gx < P.win_nb[0] * 4 && gy < P.win_nb[1] * 4 && gz < P.win_nb[2] * 4)
+        g = w.grid_vel[node_addr(P, gx, gy, gz)];
+      vt[t] = g;
+    }
+    __syncthreads();
+    for (int j = start + threadIdx.x; j < end; j += blockDim.x) {
+      float x[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) x[d] = st[(kX + d) * cap + j];
+      const int mat = __float_as_int(st[kMat * cap + j]);
+      const Base b = particle_base(P, x[0], x[1], x[2], bad);
+      float wt[3][3];
+      bspline_weights(b.fx, wt);
+      const int lx = b.b[0] - bx * 4, ly = b.b[1] - by * 4, lz = b.b[2] - bz * 4;
+      if ((unsigned)lx > 3u || (unsigned)ly > 3u || (unsigned)lz > 3u) {  // moved since binning
+        bad |= MPM_STATUS_TABLE_OVERFLOW;
+        continue;
+      }
+      // Gather, :711-721, in separable form: with t = w g,
+      //   v = sum t,  C = 4 inv_dx (sum t (x) off - v (x) fx)
+      float nv[3] = {0.f, 0.f, 0.f}, sa[3] = {0.f, 0.f, 0.f}, sb[3] = {0.f, 0.f, 0.f},
+            sc[3] = {0.f, 0.f, 0.f};
+      const int base_node = (lx * kTileW + ly) * kTileW + lz;
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int bb = 0; bb < 3; ++bb) {
+          const float wab = wt[a][0] * wt[bb][1];
+          float T[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const float4 g = vt[base_node + (a * kTileW + bb) * kTileW + c];
+            const float wgt = wab * wt[c][2];
+            const float t0 = wgt * g.x, t1 = wgt * g.y, t2 = wgt * g.z;
+            T[0] += t0;
+            T[1] += t1;
+            T[2] += t2;
+            if (c > 0) {
+              sc[0] = fmaf((float)c, t0, sc[0]);
+              sc[1] = fmaf((float)c, t1, sc[1]);
+              sc[2] = fmaf((float)c, t2, sc[2]);
+            }
+          }
+#pragma unroll
+          for (int r = 0; r < 3; ++r) {
+            nv[r] += T[r];
+            if (a > 0) sa[r] = fmaf((float)a, T[r], sa[r]);
+            if (bb > 0) sb[r] = fmaf((float)bb, T[r], sb[r]);
+          }
+        }
+      float nC[3][3];
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        nC[r][0] = s4 * fmaf(-nv[r], b.fx[0], sa[r]);
+        nC[r][1] = s4 * fmaf(-nv[r], b.fx[1], sb[r]);
+        nC[r][2] = s4 * fmaf(-nv[r], b.fx[2], sc[r]);
+      }
+      float vv[3];
+      if (mat != 4) {  // :722-724
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          vv[d] = nv[d];
+          x[d] = x[d] + dt * nv[d];
+          st[(kV + d) * cap + j] = nv[d];
+          st[(kX + d) * cap + j] = x[d];
+        }
+#pragma unroll
+        for (int a = 0; a < 9; ++a) st[(kC + a) * cap + j] = nC[a / 3][a % 3];
+      } else {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) vv[d] = st[(kV + d) * cap + j];
+      }
+      vmax = fmaxf(vmax, fmaxf(fabsf(vv[0]), fmaxf(fabsf(vv[1]), fabsf(vv[2]))));
+      bin_one(P, w, j, x[0], x[1], x[2], bad);  // next substep's build_pid
+    }
+    __syncthreads();
+  }
+  set_status(w, bad);
+  if (maxv_out) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+    if ((threadIdx.x & 31) == 0 && vmax > 0.0f) atomicMax((int *)maxv_out, __float_as_int(vmax));
+  }
+}
+
+__global__ void k_gather_rows(const float *__restrict__ ps, int64_t cap, int64_t n, int row0, int ncols,
+                              float *__restrict__ out) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const int64_t id = __float_as_int(ps[kId * cap + j]);
+  if (id < 0 || id >= n) return;  // corrupted id row: leave the slot untouched
+  for (int c = 0; c < ncols; ++c) out[id * ncols + c] = ps[(row0 + c) * cap + j];
+}
+
+// ------------------------------------------------------------ host side --
+
+struct DevInfo {
+  int sms = 0;
+  int p2g_ctas = 0, p2g_ep_ctas = 0, g2p_ctas = 0;
+};
+
+static DevInfo g_dev[64];
+static std::mutex g_dev_mu;
+
+static const DevInfo *dev_info() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lk(g_dev_mu);
+  DevInfo &d = g_dev[dev];
+  if (d.sms == 0) {
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return nullptr;
+    int a = 0, b = 0, c = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_p2g<false>, kP2GThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_p2g<true>, kP2GThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_g2p, kG2PThreads, 0);
+    d.p2g_ctas = sms * (a > 0 ? a : 1);
+    d.p2g_ep_ctas = sms * (b > 0 ? b : 1);
+    d.g2p_ctas = sms * (c > 0 ? c : 1);
+    d.sms = sms;
+  }
+  return &d;
+}
+
+static bool params_ok(const MpmParams *p) {
+  if (!p || p->version != MPM_ABI_VERSION) return false;
+  for (int d = 0; d < 3; ++d) {
+    if (p->win_nb[d] <= 0 || (p->win_lo[d] & 3) != 0) return false;
+  }
+  const int64_t nblk = (int64_t)p->win_nb[0] * p->win_nb[1] * p->win_nb[2];
+  if (nblk * kBlockCells >= (int64_t)INT32_MAX) return false;
+  if (p->chunk < 32 || (p->chunk & 31) != 0) return false;
+  if (p->n_colliders < 0 || p->n_colliders > MPM_MAX_COLLIDERS) return false;
+  return true;
+}
+
+static int last_error() { return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_E_CUDA; }
+
+}  // namespace mpm
+
+using namespace mpm;
+
+extern "C" {
+
+int mpm_abi_version(void) { return MPM_ABI_VERSION; }
+
+int mpm_workspace_bytes(const MpmParams *p, int64_t cap, size_t *bytes_out) {
+  if (!params_ok(p) || cap <= 0 || cap >= (int64_t)INT32_MAX || !bytes_out) return MPM_E_INVALID;
+  *bytes_out = ws_layout(*p, cap, nullptr, nullptr);
+  return MPM_OK;
+}
+
+int mpm_workspace_init(const MpmParams *p, void *ws, int64_t cap, void *stream) {
+  if (!params_ok(p) || !ws) return MPM_E_INVALID;
+  const size_t bytes = ws_layout(*p, cap, nullptr, nullptr);
+  if (cudaMemsetAsync(ws, 0, bytes, (cudaStream_t)stream) != cudaSuccess) return MPM_E_CUDA;
+  return MPM_OK;
+}
+
+int mpm_bin_count(const MpmParams *p, void *ws, int64_t cap, const float *pstate, int64_t begin, int64_t end,
+                  void *stream) {
+  if (!params_ok(p) || !ws || !pstate || begin < 0 || end > cap || begin > end) return MPM_E_INVALID;
+  if (end == begin) return MPM_OK;
+  Ws w;
+  ws_layout(*p, cap, (char *)ws, &w);
+  const int64_t n = end - begin;
+  k_bin_count<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(*p, w, pstate, cap, begin, end);
+  return last_error();
+}
+
+int mpm_bin_finalize(const MpmParams *p, void *ws, int64_t cap, int64_t n, void *stream) {
+  if (!params_ok(p) || !ws || n < 0 || n > cap) return MPM_E_INVALID;
+  const DevInfo *di = dev_info();
+  if (!di) return MPM_E_CUDA;
+  Ws w;
+  ws_layout(*p, cap, (char *)ws, &w);
+  cudaStream_t s = (cudaStream_t)stream;
+  k_flags_count<<<w.nflagtiles, 256, 0, s>>>(*p, w);
+  k_flags_write<<<w.nflagtiles, 256, 0, s>>>(*p, w);
+  k_pb_stats<<<w.nstattiles, 256, 0, s>>>(*p, w);
+  k_pb_scan<<<w.nstattiles, 256, 0, s>>>(*p, w);
+  k_pb_levels<<<di->sms * 8, 256, 0, s>>>(*p, w, cap);
+  if (n > 0) k_scatter<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(*p, w, n);
+  return last_error();
+}
+
+int mpm_p2g(const MpmParams *p, void *ws, int64_t cap, int64_t n, const float *cur, float *nxt, float dt,
+            void *stream) {
+  if (!params_ok(p) || !ws || !cur || !nxt || n < 0 || n > cap) return MPM_E_INVALID;
+  const DevInfo *di = dev_info();
+  if (!di) return MPM_E_CUDA;
+  Ws w;
+  ws_layout(*p, cap, (char *)ws, &w);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (p->has_Ep)
+    k_p2g<true><<<di->p2g_ep_ctas, kP2GThreads, 0, s>>>(*p, w, cur, nxt, cap, dt);
+  else
+    k_p2g<false><<<di->p2g_ctas, kP2GThreads, 0, s>>>(*p, w, cur, nxt, cap, dt);
+  return last_error();
+}
+
+int mpm_grid_update(const MpmParams *p, void *ws, int64_t cap, float dt, void *stream) {
+  if (!params_ok(p) || !ws) return MPM_E_INVALID;
+  const DevInfo *di = dev_info();
+  if (!di) return MPM_E_CUDA;
+  Ws w;
+  ws_layout(*p, cap, (char *)ws, &w);
+  k_grid<<<di->sms * 8, 256, 0, (cudaStream_t)stream>>>(*p, w, dt);
+  return last_error();
+}
+
+int mpm_g2p(const MpmParams *p, void *ws, int64_t cap, int64_t n, float *nxt, float dt, float *maxv_out,
+            void *stream) {
+  if (!params_ok(p) || !ws || !nxt || n < 0 || n > cap) return MPM_E_INVALID;
+  const DevInfo *di = dev_info();
+  if (!di) return MPM_E_CUDA;
+  Ws w;
+  ws_layout(*p, cap, (char *)ws, &w);
+  k_g2p<<<di->g2p_ctas, kG2PThreads, 0, (cudaStream_t)stream>>>(*p, w, nxt, cap, dt, maxv_out);
+  return last_error();
+}
+
+int mpm_substep(const MpmParams *p, void *ws, int64_t cap, int64_t n, const float *cur, float *nxt, float dt,
+                float *maxv_out, void *stream) {
+  int rc = mpm_bin_finalize(p, ws, cap, n, stream);
+  if (rc) return rc;
+  rc = mpm_p2g(p, ws, cap, n, cur, nxt, dt, stream);
+  if (rc) return rc;
+  rc = mpm_grid_update(p, ws, cap, dt, stream);
+  if (rc) return rc;
+  return mpm_g2p(p, ws, cap, n, nxt, dt, maxv_out, stream);
+}
+
+int mpm_gather_rows(const float *pstate, int64_t cap, int64_t n, int32_t row0, int32_t ncols, float *out,
+                    void *stream) {
+  if (!pstate || !out || n < 0 || n > cap || row0 < 0 || ncols <= 0 || row0 + ncols > MPM_NROWS)
+    return MPM_E_INVALID;
+  if (n == 0) return MPM_OK;
+  k_gather_rows<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(pstate, cap, n, row0, ncols, out);
+  return last_error();
+}
+
+int mpm_status_ptr(const MpmParams *p, void *ws, int64_t cap, uint32_t **status_out) {
+  if (!params_ok(p) || !ws || !status_out) return MPM_E_INVALID;
+  Ws w;
+  ws_layout(*p, cap, (char *)ws, &w);
+  *status_out = (uint32_t *)&w.counters[3];
+  return MPM_OK;
+}
+
+int mpm_views(const MpmParams *p, void *ws, int64_t cap, MpmViews *out) {
+  if (!params_ok(p) || !ws || !out) return MPM_E_INVALID;
+  Ws w;
+  ws_layout(*p, cap, (char *)ws, &w);
+  out->counters = w.counters;
+  out->pblocks = w.pblocks;
+  out->gblocks = w.gblocks;
+  out->pblock_count = w.pb_count;
+  out->pblock_start = w.pb_start;
+  out->pid = w.pid;
+  out->cellkey = w.cellkey;
+  out->grid_mom = (float *)w.grid_mom;
+  out->grid_vel = (float *)w.grid_vel;
+  return MPM_OK;
+}
+
+}  // extern "C"

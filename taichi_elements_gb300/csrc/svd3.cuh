@@ -1,0 +1,153 @@
+// 3x3 singular value decomposition for the P2G stress (float32, registers only).
+//
+// Replaces Taichi's ti.svd (called at engine/mpm_solver.py:525 of
+// taichi-dev/taichi_elements).  The structure follows the published method of
+// McAdams, Selle, Tamstorf, Teran and Sifakis (2011), "Computing the Singular
+// Value Decomposition of 3x3 matrices with minimal branching and elementary
+// floating point operations": symmetric eigen-analysis of A^T A by cyclic
+// Jacobi rotations, sorting of the columns of B = A V with sign-preserving
+// swaps, then a Givens QR of B.  This implementation uses exact Jacobi angles
+// (Rutishauser's formula) rather than the paper's approximate quarter angles.
+//
+// Convention (the one the reference's constitutive code relies on):
+//   A = U diag(s) V^T with U, V proper rotations (det = +1),
+//   s0 >= s1 >= |s2|, and s2 < 0 exactly when det(A) < 0.
+#pragma once
+
+namespace mpm {
+
+// 1/sqrt(x) to about 1 ulp: the hardware estimate refined by one
+// Newton-Raphson step for f(y) = 1/y^2 - x, y <- y (3 - x y^2) / 2.
+// Rotation cosines/sines built from it keep U and V orthogonal to float
+// precision, which the corotated stress 2 mu (F - U V^T) F^T needs.
+__device__ __forceinline__ float rsqrt_nr(float x) {
+  const float y = rsqrtf(x);
+  return y * fmaf(-0.5f * x * y, y, 1.5f);
+}
+
+template <int P, int Q>
+__device__ __forceinline__ void jacobi_pair(float (&S)[3][3], float (&V)[3][3]) {
+  constexpr int R = 3 - P - Q;
+  const float apq = S[P][Q];
+  if (apq != 0.0f) {
+    const float theta = (S[Q][Q] - S[P][P]) / (2.0f * apq);
+    const float at = fabsf(theta);
+    float t;
+    if (at > 1e15f) {
+      t = 0.5f / theta;
+    } else {
+      t = 1.0f / (at + sqrtf(fmaf(theta, theta, 1.0f)));
+      t = theta < 0.0f ? -t : t;
+    }
+    const float c = rsqrt_nr(fmaf(t, t, 1.0f));
+    const float s = t * c;
+    S[P][P] -= t * apq;
+    S[Q][Q] += t * apq;
+    S[P][Q] = 0.0f;
+    S[Q][P] = 0.0f;
+    const float srp = S[R][P], srq = S[R][Q];
+    S[R][P] = S[P][R] = c * srp - s * srq;
+    S[R][Q] = S[Q][R] = s * srp + c * srq;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const float vp = V[i][P], vq = V[i][Q];
+      V[i][P] = c * vp - s * vq;
+      V[i][Q] = s * vp + c * vq;
+    }
+  }
+}
+
+template <int I, int J>
+__device__ __forceinline__ void givens_qr_step(float (&B)[3][3], float (&U)[3][3]) {
+  // zero B[J][I] with a rotation of rows I and J; U accumulates G^T.
+  const float a = B[I][I], b = B[J][I];
+  const float r2 = fmaf(a, a, b * b);
+  float c = 1.0f, s = 0.0f;
+  if (r2 > 0.0f) {
+    const float ir = rsqrt_nr(r2);
+    c = a * ir;
+    s = b * ir;
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float bi = B[I][k], bj = B[J][k];
+    B[I][k] = c * bi + s * bj;
+    B[J][k] = c * bj - s * bi;
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float ui = U[k][I], uj = U[k][J];
+    U[k][I] = c * ui + s * uj;
+    U[k][J] = c * uj - s * ui;
+  }
+}
+
+template <int I, int J>
+__device__ __forceinline__ void cond_swap(bool doit, float (&B)[3][3], float (&V)[3][3], float (&rho)[3]) {
+  // swap columns I, J and negate the new column J (keeps det V = +1)
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float bi = B[k][I], bj = B[k][J];
+    B[k][I] = doit ? bj : bi;
+    B[k][J] = doit ? -bi : bj;
+    const float vi = V[k][I], vj = V[k][J];
+    V[k][I] = doit ? vj : vi;
+    V[k][J] = doit ? -vi : vj;
+  }
+  const float ri = rho[I], rj = rho[J];
+  rho[I] = doit ? rj : ri;
+  rho[J] = doit ? ri : rj;
+}
+
+template <int SWEEPS = 4>
+__device__ __forceinline__ void svd3(const float (&A)[3][3], float (&U)[3][3], float (&s)[3],
+                                     float (&V)[3][3]) {
+  float S[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = i; j < 3; ++j) {
+      float acc = A[0][i] * A[0][j];
+      acc = fmaf(A[1][i], A[1][j], acc);
+      acc = fmaf(A[2][i], A[2][j], acc);
+      S[i][j] = acc;
+      S[j][i] = acc;
+    }
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      V[i][j] = (i == j) ? 1.0f : 0.0f;
+      U[i][j] = (i == j) ? 1.0f : 0.0f;
+    }
+#pragma unroll
+  for (int sweep = 0; sweep < SWEEPS; ++sweep) {
+    jacobi_pair<0, 1>(S, V);
+    jacobi_pair<0, 2>(S, V);
+    jacobi_pair<1, 2>(S, V);
+  }
+  float B[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      float acc = A[i][0] * V[0][j];
+      acc = fmaf(A[i][1], V[1][j], acc);
+      acc = fmaf(A[i][2], V[2][j], acc);
+      B[i][j] = acc;
+    }
+  float rho[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) rho[j] = fmaf(B[0][j], B[0][j], fmaf(B[1][j], B[1][j], B[2][j] * B[2][j]));
+  cond_swap<0, 1>(rho[0] < rho[1], B, V, rho);
+  cond_swap<0, 2>(rho[0] < rho[2], B, V, rho);
+  cond_swap<1, 2>(rho[1] < rho[2], B, V, rho);
+  givens_qr_step<0, 1>(B, U);
+  givens_qr_step<0, 2>(B, U);
+  givens_qr_step<1, 2>(B, U);
+  s[0] = B[0][0];
+  s[1] = B[1][1];
+  s[2] = B[2][2];
+}
+
+}  // namespace mpm

@@ -1,0 +1,735 @@
+"""Drop-in replacement for taichi_elements' ``engine.mpm_solver.MPMSolver``.
+
+The public surface follows engine/mpm_solver.py of taichi-dev/taichi_elements:
+the constructor (:44-310), the material/surface constants (:16-42),
+``add_cube`` (:861-884), ``add_ellipsoid`` (:980-1015), ``add_particles``
+(:1097-1104), ``read_restart`` (:1128-1144), ``add_surface_collider``
+(:647-687), ``add_sphere_collider`` (:618-642), ``add_bounding_box``
+(:689-692), ``clear_grid_postprocess`` (:644-645), ``set_gravity``
+(:316-319), ``step`` (:748-821), ``particle_info`` (:1172-1191) and
+``clear_particles`` (:1193-1196).
+
+State lives in PyTorch CUDA tensors; every substep runs the hand-written
+sm_103a kernels of libmpm_gb300.so through ctypes.  There is no CPU path: a
+machine without a CUDA device, or without the built library, raises.
+
+Extensions beyond the reference: ``substep(dt)``, per-particle Young's
+modulus (``per_particle_E=True`` and the ``E`` argument of the seeding
+calls), ``state_dict``/``load_state_dict`` (exact checkpoints of x, v, C, F,
+Jp), ``tensors()`` (zero-copy device views) and CUDA-graph capture of whole
+frames.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import numbers
+import time
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import (KIND_BOX, KIND_SPHERE, KIND_SURFACE, NROWS, ROW_C, ROW_EP, ROW_F, ROW_ID, ROW_JP, ROW_MAT,
+                   ROW_V, ROW_X)
+
+
+class MPMError(RuntimeError):
+    """A device-side fault reported through the engine's status word."""
+
+
+def _ptr(t: torch.Tensor) -> int:
+    return t.data_ptr()
+
+
+class MPMSolver:
+    material_water = 0
+    material_elastic = 1
+    material_snow = 2
+    material_sand = 3
+    material_stationary = 4
+    materials = {
+        'WATER': material_water,
+        'ELASTIC': material_elastic,
+        'SNOW': material_snow,
+        'SAND': material_sand,
+        'STATIONARY': material_stationary,
+    }
+
+    surface_sticky = 0
+    surface_slip = 1
+    surface_separate = 2
+    surfaces = {'STICKY': surface_sticky, 'SLIP': surface_slip, 'SEPARATE': surface_separate}
+
+    # particles per P2G/G2P work item when the caller does not choose one
+    DEFAULT_CHUNK = 512
+    # grid nodes kept around the simulation box / particle bounding box
+    WINDOW_MARGIN = 8
+
+    def __init__(self,
+                 res,
+                 quant=False,
+                 use_voxelizer=True,
+                 size=1,
+                 max_num_particles=2**30,
+                 padding=3,
+                 unbounded=False,
+                 dt_scale=1,
+                 E_scale=1,
+                 voxelizer_super_sample=2,
+                 use_g2p2g=False,
+                 v_clamp_g2p2g=True,
+                 use_bls=True,
+                 g2p2g_allowed_cfl=0.9,
+                 water_density=1.0,
+                 support_plasticity=True,
+                 use_adaptive_dt=False,
+                 use_ggui=False,
+                 use_emitter_id=False,
+                 *,
+                 device=None,
+                 seed=0,
+                 chunk=None,
+                 use_cuda_graph=True,
+                 per_particle_E=False):
+        self.dim = len(res)
+        assert self.dim in (2, 3), "MPM solver supports only 2D and 3D simulations."
+        if self.dim != 3:
+            raise NotImplementedError("the GB300 engine implements the 3-D solver only")
+        if quant:
+            raise NotImplementedError("quantised particle storage (quant=True) is not implemented")
+        if use_g2p2g:
+            raise NotImplementedError("the fused G2P2G substep (use_g2p2g=True) is not implemented")
+        if not support_plasticity:
+            raise NotImplementedError("support_plasticity=False is not implemented")
+        if use_adaptive_dt:
+            raise NotImplementedError("adaptive dt (use_adaptive_dt=True) is not implemented")
+
+        self.device = torch.device(device if device is not None else "cuda")
+        if self.device.type != "cuda" or not torch.cuda.is_available():
+            raise RuntimeError("MPMSolver (GB300 engine) needs a CUDA device; there is no CPU path")
+        self._lib = _lib.load()
+
+        self.quant = quant
+        self.use_g2p2g = use_g2p2g
+        self.v_clamp_g2p2g = v_clamp_g2p2g
+        self.use_bls = use_bls
+        self.g2p2g_allowed_cfl = g2p2g_allowed_cfl
+        self.water_density = water_density
+        self.grid_size = 4096
+        self.t = 0.0
+        self.res = tuple(int(r) for r in res)
+        self.size = size
+        # constants: engine/mpm_solver.py:82-87
+        self.dx = size / res[0]
+        self.inv_dx = 1.0 / self.dx
+        self.default_dt = 2e-2 * self.dx / size * dt_scale
+        self.p_vol = self.dx**self.dim
+        self.p_rho = 1000
+        self.p_mass = self.p_vol * self.p_rho
+        self.max_num_particles = max_num_particles
+        self.all_time_max_velocity = 0
+        self.support_plasticity = support_plasticity
+        self.use_adaptive_dt = use_adaptive_dt
+        self.use_ggui = use_ggui
+        self.F_bound = 4.0
+        self.use_emitter_id = use_emitter_id
+        self.unbounded = unbounded
+        if unbounded:  # :143-149
+            while self.grid_size <= 2 * max(self.res):
+                self.grid_size *= 2
+        self.offset = tuple(-self.grid_size // 2 for _ in range(self.dim))
+        self.leaf_block_size = 4
+        self.padding = padding
+        # :200-210
+        self.E, self.nu = 1e6 * size * E_scale, 0.2
+        self.mu_0 = self.E / (2 * (1 + self.nu))
+        self.lambda_0 = self.E * self.nu / ((1 + self.nu) * (1 - 2 * self.nu))
+        friction_angle = math.radians(45)
+        sin_phi = math.sin(friction_angle)
+        self.alpha = math.sqrt(2 / 3) * 2 * sin_phi / (3 - sin_phi)
+        self.total_substeps = 0
+        self.voxelizer = None
+        self.voxelizer_super_sample = voxelizer_super_sample
+        self.writers = []
+
+        self.per_particle_E = bool(per_particle_E)
+        self.chunk = int(chunk) if chunk else self.DEFAULT_CHUNK
+        self.use_cuda_graph = use_cuda_graph
+        self.gravity = (0.0, -9.8, 0.0)
+        self.grid_postprocess = []  # records: dicts with kind/surface/...
+        self.add_bounding_box(self.unbounded)
+
+        self.n_particles = 0
+        self._cap = 0
+        self._state = [None, None]
+        self._cur = 0
+        self._color = None
+        self._emitter = None
+        self._ws = None
+        self._binned = 0
+        self._window = None  # (lo[3], nb[3])
+        self._params = None
+        self._params_version = 0
+        self._graphs = {}
+        self._graph_seen = set()
+        self._maxv = torch.zeros(1024, dtype=torch.float32, device=self.device)
+        self._gen = torch.Generator(device=self.device)
+        self._gen.manual_seed(int(seed))
+        self._seed_lo = None  # bounding box (in nodes) of all seeded regions
+        self._seed_hi = None
+        self._set_window(*self._box_window())
+
+    # ---------------------------------------------------------- params ---
+
+    def _box_window(self):
+        m = self.WINDOW_MARGIN
+        lo = [(-m // 4) * 4] * 3
+        hi = [r + m for r in self.res]
+        return lo, hi
+
+    def _set_window(self, lo, hi):
+        lo = [int(math.floor(l / 4.0)) * 4 for l in lo]
+        nb = [int(math.ceil((h - l) / 4.0)) for l, h in zip(lo, hi)]
+        self._window = (lo, nb)
+        self._params = None
+
+    def _build_params(self) -> _lib.MpmParams:
+        p = _lib.MpmParams()
+        p.version = _lib.ABI_VERSION
+        for d in range(3):
+            p.res[d] = self.res[d]
+            p.win_lo[d] = self._window[0][d]
+            p.win_nb[d] = self._window[1][d]
+        p.padding = self.padding
+        p.unbounded = int(bool(self.unbounded))
+        p.grid_size = self.grid_size
+        p.has_Ep = int(self.per_particle_E)
+        p.chunk = self.chunk
+        p.dx = self.dx
+        p.inv_dx = self.inv_dx
+        p.p_vol = self.p_vol
+        p.p_mass = self.p_mass
+        p.mu0 = self.mu_0
+        p.la0 = self.lambda_0
+        p.nu = self.nu
+        p.alpha = self.alpha
+        p.water_density = self.water_density
+        for d in range(3):
+            p.gravity[d] = self.gravity[d]
+        p.stress_k = self.p_vol * 4 * self.inv_dx**2
+        p.sand_k = (self.dim * self.lambda_0 + 2 * self.mu_0) / (2 * self.mu_0)
+        if len(self.grid_postprocess) > _lib.MAX_COLLIDERS:
+            raise ValueError(f"at most {_lib.MAX_COLLIDERS} grid post-process entries are supported")
+        p.n_colliders = len(self.grid_postprocess)
+        for i, c in enumerate(self.grid_postprocess):
+            r = p.colliders[i]
+            r.kind = c["kind"]
+            r.surface = c["surface"]
+            for d in range(3):
+                r.point[d] = c.get("point", (0, 0, 0))[d]
+                r.normal[d] = c.get("normal", (0, 0, 0))[d]
+            r.radius = c.get("radius", 0.0)
+            r.friction = c.get("friction", 0.0)
+        return p
+
+    @property
+    def params(self) -> _lib.MpmParams:
+        if self._params is None:
+            self._params = self._build_params()
+            self._params_version += 1
+            self._graphs.clear()
+        return self._params
+
+    def _invalidate_params(self):
+        self._params = None
+
+    def set_gravity(self, g):
+        assert isinstance(g, (tuple, list))
+        assert len(g) == self.dim
+        self.gravity = tuple(float(x) for x in g)
+        self._invalidate_params()
+
+    # -------------------------------------------------------- colliders ---
+
+    def add_sphere_collider(self, center, radius, surface=surface_sticky):
+        center = list(center)
+        self.grid_postprocess.append(
+            dict(kind=KIND_SPHERE, surface=int(surface), point=tuple(center), radius=float(radius)))
+        self._invalidate_params()
+
+    def clear_grid_postprocess(self):
+        self.grid_postprocess.clear()
+        self._invalidate_params()
+
+    def add_surface_collider(self, point, normal, surface=surface_sticky, friction=0.0):
+        point = list(point)
+        normal_scale = 1.0 / math.sqrt(sum(x**2 for x in normal))
+        normal = list(normal_scale * x for x in normal)
+        if surface == self.surface_sticky and friction != 0:
+            raise ValueError('friction must be 0 on sticky surfaces.')
+        self.grid_postprocess.append(
+            dict(kind=KIND_SURFACE, surface=int(surface), point=tuple(point), normal=tuple(normal),
+                 friction=float(friction)))
+        self._invalidate_params()
+
+    def add_bounding_box(self, unbounded):
+        self.grid_postprocess.append(dict(kind=KIND_BOX, surface=int(bool(unbounded))))
+        self._invalidate_params()
+
+    # ------------------------------------------------------ allocation ---
+
+    @property
+    def stream(self) -> int:
+        return torch.cuda.current_stream(self.device).cuda_stream
+
+    def _alloc(self, cap: int):
+        """(Re)allocate particle buffers with capacity `cap`, keeping data."""
+        cap = int((cap + 255) // 256 * 256)
+        n = self.n_particles
+        new_state = [torch.zeros((NROWS, cap), dtype=torch.float32, device=self.device) for _ in range(2)]
+        new_color = torch.zeros(cap, dtype=torch.int32, device=self.device)
+        new_emit = torch.zeros(cap, dtype=torch.int32, device=self.device)
+        if n > 0:
+            new_state[0][:, :n] = self._state[self._cur][:, :n]
+            new_color[:n] = self._color[:n]
+            new_emit[:n] = self._emitter[:n]
+        self._state = new_state
+        self._cur = 0
+        self._color = new_color
+        self._emitter = new_emit
+        self._cap = cap
+        self._ws = None  # workspace depends on the capacity
+        self._graphs.clear()
+
+    def _ensure_workspace(self):
+        if self._ws is not None:
+            return
+        p = self.params
+        nbytes = ctypes.c_size_t(0)
+        _lib.check(self._lib.mpm_workspace_bytes(ctypes.byref(p), self._cap, ctypes.byref(nbytes)),
+                   "mpm_workspace_bytes")
+        self._ws = torch.empty(int(nbytes.value), dtype=torch.uint8, device=self.device)
+        _lib.check(self._lib.mpm_workspace_init(ctypes.byref(p), _ptr(self._ws), self._cap, self.stream),
+                   "mpm_workspace_init")
+        sp = ctypes.c_void_p(0)
+        _lib.check(self._lib.mpm_status_ptr(ctypes.byref(p), _ptr(self._ws), self._cap, ctypes.byref(sp)),
+                   "mpm_status_ptr")
+        off = sp.value - _ptr(self._ws)
+        self._status = self._ws[off:off + 4].view(torch.int32)
+        self._binned = 0
+        self._graphs.clear()
+
+    def _ensure_capacity(self, extra: int):
+        need = self.n_particles + extra
+        if need > self._cap:
+            cap = max(need, 2 * self._cap, 1 << 16)
+            cap = min(cap, max(self.max_num_particles, need))
+            self._alloc(cap)
+
+    def _cover(self, lo_pos, hi_pos):
+        """Grow the grid window so positions in [lo_pos, hi_pos] keep their
+        stencils inside it with the margin."""
+        m = self.WINDOW_MARGIN
+        wlo, wnb = self._window
+        whi = [l + 4 * b for l, b in zip(wlo, wnb)]
+        # non-finite coordinates do not move the window; the kernels flag them
+        lo_n = [int(math.floor(l * self.inv_dx)) - m if math.isfinite(l) else wl for l, wl in zip(lo_pos, wlo)]
+        hi_n = [int(math.ceil(h * self.inv_dx)) + m if math.isfinite(h) else wh for h, wh in zip(hi_pos, whi)]
+        if all(a >= b for a, b in zip(lo_n, wlo)) and all(a <= b for a, b in zip(hi_n, whi)):
+            return
+        half = self.grid_size // 2
+        new_lo = [max(-half, min(a, b)) for a, b in zip(lo_n, wlo)]
+        new_hi = [min(half, max(a, b)) for a, b in zip(hi_n, whi)]
+        self._set_window(new_lo, new_hi)
+        self._ws = None
+
+    def _rebin(self):
+        """Bin particles that are not binned yet (all after a workspace reset)."""
+        self._ensure_workspace()
+        if self._binned < self.n_particles:
+            p = self.params
+            _lib.check(
+                self._lib.mpm_bin_count(ctypes.byref(p), _ptr(self._ws), self._cap, _ptr(self._state[self._cur]),
+                                        self._binned, self.n_particles, self.stream), "mpm_bin_count")
+            self._binned = self.n_particles
+
+    # ---------------------------------------------------------- seeding ---
+
+    def _append(self, x: torch.Tensor, material, color, velocity, emitter_id=0, E=None):
+        """Append particles with positions x (n,3) float32 on the device.
+        engine/mpm_solver.py:823-838 (seed_particle): F = I, C = 0,
+        Jp = 0 for sand and 1 otherwise, v = source velocity."""
+        n = int(x.shape[0])
+        if n == 0:
+            return
+        assert self.n_particles + n <= self.max_num_particles
+        self._ensure_capacity(n)
+        s = self._state[self._cur]
+        si = s.view(torch.int32)
+        a, b = self.n_particles, self.n_particles + n
+        s[ROW_X:ROW_X + 3, a:b] = x.t()
+        if isinstance(velocity, torch.Tensor):
+            s[ROW_V:ROW_V + 3, a:b] = velocity.to(self.device, torch.float32).t()
+        else:
+            vel = [0.0, 0.0, 0.0] if velocity is None else list(velocity)
+            assert len(vel) == self.dim
+            for d in range(3):
+                s[ROW_V + d, a:b] = float(np.float32(vel[d]))
+        s[ROW_C:ROW_C + 9, a:b] = 0.0
+        s[ROW_F:ROW_F + 9, a:b] = 0.0
+        for d in range(3):
+            s[ROW_F + 4 * d, a:b] = 1.0
+        if isinstance(material, torch.Tensor):
+            mat = material.to(self.device, torch.int32)
+            si[ROW_MAT, a:b] = mat
+            s[ROW_JP, a:b] = torch.where(mat == self.material_sand, 0.0, 1.0)
+        else:
+            si[ROW_MAT, a:b] = int(material)
+            s[ROW_JP, a:b] = 0.0 if int(material) == self.material_sand else 1.0
+        si[ROW_ID, a:b] = torch.arange(a, b, dtype=torch.int32, device=self.device)
+        if self.per_particle_E:
+            if E is None:
+                s[ROW_EP, a:b] = float(self.E)
+            elif isinstance(E, torch.Tensor):
+                s[ROW_EP, a:b] = E.to(self.device, torch.float32)
+            else:
+                s[ROW_EP, a:b] = float(E)
+        if isinstance(color, torch.Tensor):
+            self._color[a:b] = color.to(self.device, torch.int32)
+        else:
+            self._color[a:b] = int(np.array(int(color), dtype=np.int64).astype(np.int32))
+        self._emitter[a:b] = int(emitter_id)
+        self.n_particles = b
+        # bin the new particles (the window may have grown: that rebins all)
+        self._rebin()
+
+    def _note_region(self, lo, hi):
+        self._cover(lo, hi)
+
+    @staticmethod
+    def _finite_bounds(x: torch.Tensor):
+        """Per-axis min/max over the finite entries of an (n,3) tensor."""
+        fin = torch.isfinite(x)
+        lo = torch.where(fin, x, torch.full_like(x, float('inf'))).min(0).values
+        hi = torch.where(fin, x, torch.full_like(x, float('-inf'))).max(0).values
+        return lo.tolist(), hi.tolist()
+
+    def add_cube(self, lower_corner, cube_size, material, color=0xFFFFFF, sample_density=None, velocity=None,
+                 E=None):
+        """engine/mpm_solver.py:861-884; positions lower + U[0,1) * size."""
+        if sample_density is None:
+            sample_density = 2**self.dim
+        vol = 1
+        for i in range(self.dim):
+            vol = vol * cube_size[i]
+        num_new_particles = int(sample_density * vol / self.dx**self.dim + 1)
+        assert self.n_particles + num_new_particles <= self.max_num_particles
+        lo = torch.tensor([float(v) for v in lower_corner], dtype=torch.float32, device=self.device)
+        sz = torch.tensor([float(v) for v in cube_size], dtype=torch.float32, device=self.device)
+        u = torch.rand((num_new_particles, 3), generator=self._gen, device=self.device, dtype=torch.float32)
+        x = lo + u * sz
+        self._note_region([float(a) for a in lower_corner],
+                          [float(a) + float(b) for a, b in zip(lower_corner, cube_size)])
+        self._append(x, material, color, velocity, E=E)
+
+    def add_ellipsoid(self, center, radius, material, color=0xFFFFFF, sample_density=None, velocity=None, E=None):
+        """engine/mpm_solver.py:980-1015 with rejection sampling in the unit
+        sphere (:959-967)."""
+        if sample_density is None:
+            sample_density = 2**self.dim
+        if isinstance(radius, numbers.Number):
+            radius = [radius] * self.dim
+        radius = list(radius)
+        num_particles = 4 / 3 * math.pi
+        for i in range(self.dim):
+            num_particles *= radius[i] * self.inv_dx
+        num_particles = int(math.ceil(num_particles * sample_density))
+        assert self.n_particles + num_particles <= self.max_num_particles
+        pts = []
+        have = 0
+        while have < num_particles:
+            m = max(64, int((num_particles - have) * 2.1) + 64)
+            u = torch.rand((m, 3), generator=self._gen, device=self.device, dtype=torch.float32) * 2 - 1
+            u = u[(u * u).sum(1) <= 1]
+            pts.append(u)
+            have += int(u.shape[0])
+        u = torch.cat(pts)[:num_particles]
+        c = torch.tensor([float(v) for v in center], dtype=torch.float32, device=self.device)
+        r = torch.tensor([float(v) for v in radius], dtype=torch.float32, device=self.device)
+        x = c + u * r
+        self._note_region([float(a) - float(b) for a, b in zip(center, radius)],
+                          [float(a) + float(b) for a, b in zip(center, radius)])
+        self._append(x, material, color, velocity, E=E)
+
+    def add_particles(self, particles, material, color=0xFFFFFF, velocity=None, E=None):
+        """engine/mpm_solver.py:1081-1104."""
+        x = torch.as_tensor(np.asarray(particles, dtype=np.float32)).reshape(-1, 3)
+        if x.shape[0] == 0:
+            return
+        self._note_region(*self._finite_bounds(x))
+        self._append(x.to(self.device), material, color, velocity, E=E)
+
+    def read_restart(self, num_particles, pos, vel, material, color):
+        """engine/mpm_solver.py:1106-1144 (per-particle x, v, material,
+        color; F = I, Jp reset, C = 0)."""
+        num_particles = int(num_particles)
+        if num_particles == 0:
+            return
+        x = torch.as_tensor(np.asarray(pos[:num_particles], dtype=np.float32)).reshape(-1, 3)
+        v = torch.as_tensor(np.asarray(vel[:num_particles], dtype=np.float32)).reshape(-1, 3)
+        m = torch.as_tensor(np.asarray(material[:num_particles]).astype(np.int32))
+        c = torch.as_tensor(np.asarray(color[:num_particles]).astype(np.int64).astype(np.int32))
+        self._note_region(*self._finite_bounds(x))
+        self._append(x.to(self.device), m, c, v, E=None)
+
+    def add_mesh(self, *args, **kwargs):
+        raise NotImplementedError("add_mesh (voxelizer emitter) is not part of the GB300 engine")
+
+    def add_ngon(self, *args, **kwargs):
+        raise ValueError("Add Ngon only works for 2D simulations")
+
+    def add_texture_2d(self, *args, **kwargs):
+        raise NotImplementedError("2-D texture seeding is not part of the 3-D GB300 engine")
+
+    def clear_particles(self):
+        """engine/mpm_solver.py:1193-1196."""
+        self.n_particles = 0
+        self._binned = 0
+        self._ws = None
+
+    # ------------------------------------------------------------- step ---
+
+    def _check_window_covers_particles(self, frame_dt: float):
+        """Grow the grid window if particles got close to its edge."""
+        if self.n_particles == 0:
+            return
+        x = self._state[self._cur][ROW_X:ROW_X + 3, :self.n_particles]
+        mn, mx = self._finite_bounds(x.t())
+        reach = (max(self.all_time_max_velocity, 1.0) * frame_dt * 2.0)
+        self._cover([a - reach for a in mn], [b + reach for b in mx])
+        if self._ws is None:
+            self._rebin()
+
+    def _check_status(self):
+        st = int(self._status.item())
+        if st:
+            self._status.zero_()
+            msgs = []
+            if st & _lib.STATUS_OUT_OF_GRID:
+                msgs.append("particles left the grid window (their stencils were clamped)")
+            if st & _lib.STATUS_NONFINITE:
+                msgs.append("non-finite particle positions")
+            if st & _lib.STATUS_TABLE_OVERFLOW:
+                msgs.append("binning tables inconsistent (stale particle binning)")
+            raise MPMError("MPM device status: " + "; ".join(msgs))
+
+    def _launch_substep(self, dt: float, maxv_slot: int):
+        p = self.params
+        cur = self._state[self._cur]
+        nxt = self._state[1 - self._cur]
+        mv = _ptr(self._maxv) + 4 * maxv_slot if maxv_slot >= 0 else None
+        _lib.check(
+            self._lib.mpm_substep(ctypes.byref(p), _ptr(self._ws), self._cap, self.n_particles, _ptr(cur), _ptr(nxt),
+                                  float(dt), mv, self.stream), "mpm_substep")
+        self._cur = 1 - self._cur
+
+    def _prepare(self, frame_dt: float = 0.0):
+        self._ensure_workspace()
+        self._rebin()
+        self._check_window_covers_particles(frame_dt)
+        self._ensure_workspace()
+        self._rebin()
+
+    def substep(self, dt: float):
+        """One substep (engine/mpm_solver.py:789-797) with time step dt."""
+        self._prepare(dt)
+        if self.n_particles == 0:
+            self.t += dt
+            return
+        self._maxv[:1].zero_()
+        self._launch_substep(dt, 0)
+        self.t += dt
+        self.total_substeps += 1
+
+    @staticmethod
+    def count_substeps(frame_dt: float, default_dt: float):
+        """Substep count and dt of engine/mpm_solver.py:752-771 (including the
+        float64 loop that can run one more substep than `substeps`)."""
+        substeps = int(frame_dt / default_dt) + 1
+        dt = frame_dt / substeps
+        frame_time_left = frame_dt
+        count = 0
+        while frame_time_left > 0:
+            count += 1
+            frame_time_left -= dt
+        return count, dt
+
+    def _run_frame(self, count: int, dt: float):
+        """Run `count` substeps, through a CUDA graph when enabled."""
+        if count > self._maxv.numel():
+            self._maxv = torch.zeros(count, dtype=torch.float32, device=self.device)
+        key = (count, float(dt), self._cur, self.n_particles, self._params_version, _ptr(self._ws))
+        if not self.use_cuda_graph:
+            self._maxv[:count].zero_()
+            for s in range(count):
+                self._launch_substep(dt, s)
+            return
+        g = self._graphs.get(key)
+        if g is None and key in self._graph_seen:
+            start_cur = self._cur
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                self._maxv[:count].zero_()
+                for s in range(count):
+                    self._launch_substep(dt, s)
+            self._cur = start_cur  # capture does not execute
+            self._graphs[key] = g
+        if g is not None:
+            g.replay()
+            self._cur = (self._cur + count) % 2
+            return
+        self._graph_seen.add(key)
+        self._maxv[:count].zero_()
+        for s in range(count):
+            self._launch_substep(dt, s)
+
+    def step(self, frame_dt, print_stat=False, smry_writer=None):
+        """engine/mpm_solver.py:748-821."""
+        begin_t = time.time()
+        begin_substep = self.total_substeps
+        count, dt = self.count_substeps(frame_dt, self.default_dt)
+        if print_stat:
+            print(f'needed substeps: {int(frame_dt / self.default_dt) + 1}')
+        self._prepare(frame_dt)
+        if self.n_particles > 0:
+            self._run_frame(count, dt)
+            maxv = self._maxv[:count].cpu().numpy()
+            self._check_status()
+        else:
+            maxv = np.zeros(count, dtype=np.float32)
+        for s in range(count):
+            self.total_substeps += 1
+            self.t += dt
+            if smry_writer is not None:
+                smry_writer.add_scalar("substep_max_CFL", float(maxv[s]) * dt / self.dx, self.total_substeps)
+        if count:
+            self.all_time_max_velocity = max(self.all_time_max_velocity, float(maxv.max()))
+        if print_stat:
+            cur_frame_velocity = float(maxv[-1]) if count else 0.0
+            print(f'CFL: {cur_frame_velocity * dt / self.dx}')
+            print(f'num particles={self.n_particles}')
+            print(f'  frame time {time.time() - begin_t:.3f} s')
+            print(f'  substep time {1000 * (time.time() - begin_t) / max(1, self.total_substeps - begin_substep):.3f} ms')
+
+    # --------------------------------------------------------- readback ---
+
+    def _gather(self, row0: int, ncols: int) -> torch.Tensor:
+        n = self.n_particles
+        out = torch.empty((n, ncols), dtype=torch.float32, device=self.device)
+        if n:
+            _lib.check(
+                self._lib.mpm_gather_rows(_ptr(self._state[self._cur]), self._cap, n, row0, ncols, _ptr(out),
+                                          self.stream), "mpm_gather_rows")
+        return out
+
+    def particle_info(self):
+        """engine/mpm_solver.py:1172-1191: copies in original particle order."""
+        n = self.n_particles
+        data = {
+            'position': self._gather(ROW_X, 3).cpu().numpy(),
+            'velocity': self._gather(ROW_V, 3).cpu().numpy(),
+            'material': self._gather(ROW_MAT, 1).view(torch.int32).reshape(n).cpu().numpy(),
+            'color': self._color[:n].cpu().numpy() if n else np.zeros(0, np.int32),
+        }
+        if self.use_emitter_id:
+            data['emitter_ids'] = self._emitter[:n].cpu().numpy() if n else np.zeros(0, np.int32)
+        return data
+
+    def full_state(self):
+        """All particle fields in original order as float32 device tensors:
+        x (n,3), v (n,3), C (n,3,3), F (n,3,3), Jp (n,), material (n,) int32."""
+        n = self.n_particles
+        g = self._gather(0, ROW_ID)
+        return {
+            'x': g[:, ROW_X:ROW_X + 3],
+            'v': g[:, ROW_V:ROW_V + 3],
+            'C': g[:, ROW_C:ROW_C + 9].reshape(n, 3, 3),
+            'F': g[:, ROW_F:ROW_F + 9].reshape(n, 3, 3),
+            'Jp': g[:, ROW_JP],
+            'material': g[:, ROW_MAT].contiguous().view(torch.int32),
+        }
+
+    def state_dict(self):
+        st = {k: v.clone() for k, v in self.full_state().items()}
+        st['color'] = self._color[:self.n_particles].clone()
+        st['t'] = self.t
+        st['total_substeps'] = self.total_substeps
+        return st
+
+    def load_state_dict(self, st):
+        """Replace all particles by an exact checkpoint from state_dict()."""
+        self.clear_particles()
+        x = st['x'].to(self.device, torch.float32)
+        n = int(x.shape[0])
+        lo = x.min(0).values.tolist() if n else [0, 0, 0]
+        hi = x.max(0).values.tolist() if n else [0, 0, 0]
+        if n:
+            self._note_region(lo, hi)
+            self._append(x, st['material'], st['color'], st['v'])
+            s = self._state[self._cur]
+            s[ROW_C:ROW_C + 9, :n] = st['C'].reshape(n, 9).t().to(self.device)
+            s[ROW_F:ROW_F + 9, :n] = st['F'].reshape(n, 9).t().to(self.device)
+            s[ROW_JP, :n] = st['Jp'].to(self.device)
+        self.t = st.get('t', 0.0)
+        self.total_substeps = st.get('total_substeps', 0)
+
+    def tensors(self):
+        """Zero-copy views of the current (sorted) particle state rows."""
+        n = self.n_particles
+        s = self._state[self._cur]
+        return {
+            'x': s[ROW_X:ROW_X + 3, :n],
+            'v': s[ROW_V:ROW_V + 3, :n],
+            'C': s[ROW_C:ROW_C + 9, :n],
+            'F': s[ROW_F:ROW_F + 9, :n],
+            'Jp': s[ROW_JP, :n],
+            'material': s.view(torch.int32)[ROW_MAT, :n],
+            'id': s.view(torch.int32)[ROW_ID, :n],
+        }
+
+    def views(self):
+        """Device views of the engine's binning and grid arrays (diagnostics
+        and parity tests): counters, particle-block and grid-block lists (as
+        window-linear block indices), per-particle-block counts and starts, the
+        sorted order, cell keys, and the momentum / velocity grids as (nodes, 4)
+        float32 in window block-major order."""
+        self._ensure_workspace()
+        p = self.params
+        v = _lib.MpmViews()
+        _lib.check(self._lib.mpm_views(ctypes.byref(p), _ptr(self._ws), self._cap, ctypes.byref(v)), "mpm_views")
+        base = _ptr(self._ws)
+        nb = self._window[1]
+        nblk = nb[0] * nb[1] * nb[2]
+
+        def sl(addr, count, dtype, width=1):
+            off = addr - base
+            t = self._ws[off:off + count * width * 4].view(dtype)
+            return t.view(count, width) if width > 1 else t
+
+        return {
+            'counters': sl(v.counters, 32, torch.int32),
+            'pblocks': sl(v.pblocks, nblk, torch.int32),
+            'gblocks': sl(v.gblocks, nblk, torch.int32),
+            'pblock_count': sl(v.pblock_count, nblk, torch.int32),
+            'pblock_start': sl(v.pblock_start, nblk, torch.int32),
+            'pid': sl(v.pid, self._cap, torch.int32),
+            'cellkey': sl(v.cellkey, self._cap, torch.int32),
+            'grid_mom': sl(v.grid_mom, nblk * 64, torch.float32, 4),
+            'grid_vel': sl(v.grid_vel, nblk * 64, torch.float32, 4),
+            'win_lo': list(self._window[0]),
+            'win_nb': list(nb),
+        }
+
+    def write_particles(self, fn, slice_size=1000000):
+        raise NotImplementedError("particle file output is not part of the GB300 engine")

@@ -1,0 +1,78 @@
+"""Shared helpers of the parity tests: oracle configs for scenes, block and
+node coordinate conversion of the engine's window layout, tolerance norms."""
+import ctypes
+
+import numpy as np
+
+from oracle import oracle as O
+
+
+def oracle_config(scene_or_solver, gravity=(0.0, -9.8, 0.0)):
+    """oracle.Config with the same constants and post-process list."""
+    s = scene_or_solver
+    if hasattr(s, "grid_postprocess"):
+        pp = []
+        for c in s.grid_postprocess:
+            d = dict(c)
+            pp.append(d)
+        return O.Config(res=s.res, size=s.size if hasattr(s, "size") else 1.0, gravity=tuple(s.gravity),
+                        postprocess=pp, unbounded=s.unbounded, water_density=s.water_density,
+                        padding=s.padding)
+    pp = [dict(kind=O.KIND_BOX, surface=0)] + list(s.postprocess)
+    return O.Config(res=s.res, size=s.size, gravity=gravity, postprocess=pp, E_scale=getattr(s, "E_scale", 1.0))
+
+
+def block_coords(lin, win_lo, win_nb):
+    """Window-linear 4^3 block indices -> global block coordinates (k,3)."""
+    lin = np.asarray(lin, dtype=np.int64)
+    bz = lin % win_nb[2]
+    by = (lin // win_nb[2]) % win_nb[1]
+    bx = lin // (win_nb[1] * win_nb[2])
+    return np.stack([bx, by, bz], 1) + np.asarray(win_lo)[None] // 4
+
+
+def node_coords(gblocks_lin, win_lo, win_nb):
+    """Global node coordinates of all nodes of the given blocks, in the
+    engine's block-major node order: (k*64, 3)."""
+    b = block_coords(gblocks_lin, win_lo, win_nb)
+    l = np.arange(64)
+    loc = np.stack([l >> 4, (l >> 2) & 3, l & 3], 1)
+    return (b[:, None, :] * 4 + loc[None]).reshape(-1, 3)
+
+
+def gpu_grid(views, which):
+    """(coords (K,3), values (K,4)) of the grid-active nodes."""
+    import torch
+    ng = int(views['counters'][1].item())
+    gb = views['gblocks'][:ng].cpu().numpy()
+    coords = node_coords(gb, views['win_lo'], views['win_nb'])
+    addr = (gb[:, None].astype(np.int64) * 64 + np.arange(64)[None]).reshape(-1)
+    vals = views[which][torch.as_tensor(addr, device=views[which].device)].cpu().numpy()
+    return coords, vals
+
+
+def window_lookup(win, coords, arr):
+    idx = tuple((coords - win.lo[None]).T)
+    return arr[idx]
+
+
+def rel_inf(a, b, scale=None):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    s = np.abs(b).max() if scale is None else scale
+    return float(np.abs(a - b).max() / max(s, 1e-30))
+
+
+def particles_from_solver(solver, dtype=np.float64):
+    """Oracle Particles (original order) from an engine's state."""
+    st = solver.full_state()
+    return O.Particles(st['x'].cpu().numpy().astype(dtype), st['v'].cpu().numpy().astype(dtype),
+                       st['C'].cpu().numpy().astype(dtype), st['F'].cpu().numpy().astype(dtype),
+                       st['Jp'].cpu().numpy().astype(dtype), st['material'].cpu().numpy().astype(np.int32))
+
+
+def lib_call(solver, name, *args):
+    from taichi_elements_gb300 import _lib
+    p = solver.params
+    rc = getattr(solver._lib, name)(ctypes.byref(p), *args)
+    _lib.check(rc, name)

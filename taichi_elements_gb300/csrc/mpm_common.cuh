@@ -35,7 +35,7 @@ struct Ws {
   unsigned long long *lvl_mask;  // [cap]
   int32_t *lvl_L;                // [cap]
   int2 *items;                   // [cap/32 + nblk + 1]
-  int32_t *cellkey, *rank, *pid;  // [cap]
+  int32_t *cellkey, *pid;  // [cap]
   int32_t *cell_cnt;              // [nblk * 64]
   float4 *grid_mom;               // [nblk * 64] (m, mv)
   float4 *grid_vel;               // [nblk * 64] (v, m)
@@ -75,7 +75,6 @@ inline size_t ws_layout(const MpmParams &p, int64_t cap, char *base, Ws *w) {
   t.lvl_L = (int32_t *)take((size_t)cap * 4);
   t.items = (int2 *)take((size_t)items_cap * 8);
   t.cellkey = (int32_t *)take((size_t)cap * 4);
-  t.rank = (int32_t *)take((size_t)cap * 4);
   t.pid = (int32_t *)take((size_t)cap * 4);
   t.cell_cnt = (int32_t *)take((size_t)nblk * kBlockCells * 4);
   t.grid_mom = (float4 *)take((size_t)nblk * kBlockCells * 16);
@@ -132,11 +131,16 @@ __device__ __forceinline__ int block_linear(const MpmParams &P, int bx, int by, 
   return (bx * P.win_nb[1] + by) * P.win_nb[2] + bz;
 }
 
+// Cell index inside a 4^3 block, ordered y, x, z.  Eight consecutive cells
+// (one quarter-warp of 128-bit shared-memory accesses in rank-major order)
+// then cover x in {2k, 2k+1} and z in 0..3, whose 6^3-tile nodes fall in
+// eight different 16-byte bank groups (x stride 36 = 4 mod 8).
+__device__ __forceinline__ int local_cell(int lx, int ly, int lz) { return (ly * 4 + lx) * 4 + lz; }
+
 // Key of the particle's cell: window block * 64 + cell within the block.
 __device__ __forceinline__ int cell_key(const MpmParams &P, const Base &b) {
   const int blin = block_linear(P, b.b[0] >> 2, b.b[1] >> 2, b.b[2] >> 2);
-  const int cell = ((b.b[0] & 3) * 4 + (b.b[1] & 3)) * 4 + (b.b[2] & 3);
-  return blin * kBlockCells + cell;
+  return blin * kBlockCells + local_cell(b.b[0] & 3, b.b[1] & 3, b.b[2] & 3);
 }
 
 // Grid node address (float4 index) of a window-relative node.
@@ -216,6 +220,29 @@ __device__ __forceinline__ P2GOut constitutive(const MpmParams &P, float dt, int
     Fn[0][0] = J;
     Jp = J;
   } else {
+    if (mat == 1 || mat == 4) {
+      // Elastic and stationary particles never clamp sigma (:527-536), so
+      // J = s0*s1*s2 = det(Fn) and the corotated stress needs only the
+      // rotation R = U V^T, which for det Fn > 0 is the polar factor.
+      // Inverted or extremely stretched Fn takes the SVD below, which keeps
+      // the reference's rotation-only convention for det Fn < 0.
+      const float J = Fn[0][0] * (Fn[1][1] * Fn[2][2] - Fn[1][2] * Fn[2][1]) -
+                      Fn[0][1] * (Fn[1][0] * Fn[2][2] - Fn[1][2] * Fn[2][0]) +
+                      Fn[0][2] * (Fn[1][0] * Fn[2][1] - Fn[1][1] * Fn[2][0]);
+      float R[3][3];
+      if (J > 0.0f && polar_rotation<5>(Fn, R)) {
+        const float lj = la * J * (J - 1.0f);
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            const float acc = (Fn[i][0] - R[i][0]) * Fn[j][0] + (Fn[i][1] - R[i][1]) * Fn[j][1] +
+                              (Fn[i][2] - R[i][2]) * Fn[j][2];
+            stress[i][j] = 2.0f * mu * acc + ((i == j) ? lj : 0.0f);
+          }
+        goto done;
+      }
+    }
     float U[3][3], sg[3], V[3][3];
     svd3<4>(Fn, U, sg, V);
     if (mat != 3) {
@@ -298,6 +325,7 @@ __device__ __forceinline__ P2GOut constitutive(const MpmParams &P, float dt, int
           stress[i][j] = T[i][0] * Fn[j][0] + T[i][1] * Fn[j][1] + T[i][2] * Fn[j][2];
     }
   }
+done:
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll

@@ -48,7 +48,7 @@ __device__ __forceinline__ void bin_one(const MpmParams &P, const Ws &w, int64_t
                                         float x2, uint32_t &bad) {
   const Base b = particle_base(P, x0, x1, x2, bad);
   const int key = cell_key(P, b);
-  const int r = atomicAdd(&w.cell_cnt[key], 1);
+  atomicAdd(&w.cell_cnt[key], 1);  // result unused: a fire-and-forget reduction
   const int blin = key >> 6;
   // Blocks this particle's 3^3 stencil reaches: its own block plus, per axis,
   // the next block when the base sits in the last two cells of the block.
@@ -59,7 +59,6 @@ __device__ __forceinline__ void bin_one(const MpmParams &P, const Ws &w, int64_t
   const int mask = kNeighbourMask[need];
   if ((w.blk_flag[blin] & mask) != mask) atomicOr(&w.blk_flag[blin], mask);
   w.cellkey[i] = key;
-  w.rank[i] = r;
 }
 
 __global__ void k_bin_count(const MpmParams P, const Ws w, const float *__restrict__ ps, int64_t cap,
@@ -283,8 +282,7 @@ __global__ __launch_bounds__(256) void k_pb_levels(const MpmParams P, const Ws w
       else
         set_status(w, MPM_STATUS_TABLE_OVERFLOW);
     }
-    cc[lane] = 0;
-    cc[lane + 32] = 0;
+    // the cell counters are counted back to zero by k_scatter
     if (lane == 0) w.blk_flag[blin] = 0;
   }
 }
@@ -293,7 +291,9 @@ __global__ void k_scatter(const MpmParams P, const Ws w, int64_t n) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int key = w.cellkey[i];
-  const int r = w.rank[i];
+  // rank inside the cell: count the cell's counter back down (this also
+  // leaves it zero for the next binning pass)
+  const int r = atomicSub(&w.cell_cnt[key], 1) - 1;
   const int blin = key >> 6, c = key & 63;
   const int k = w.blk_slot[blin];
   if (k < 0 || k >= w.counters[0] || r < 0) {  // stale binning: report, never index out of range
@@ -401,7 +401,7 @@ __global__ __launch_bounds__(kP2GThreads, 5) void k_p2g(const MpmParams P, const
           bad |= MPM_STATUS_TABLE_OVERFLOW;
           active = false;
         } else {
-          cell = (lx * 4 + ly) * 4 + lz;
+          cell = local_cell(lx, ly, lz);
           bspline_weights(b.fx, wt);
           mass = o.mass;
           // APIC scatter, :576-584: node value = w * (m v + A (off - fx) dx)

@@ -30,13 +30,17 @@ __device__ __forceinline__ void jacobi_pair(float (&S)[3][3], float (&V)[3][3]) 
   constexpr int R = 3 - P - Q;
   const float apq = S[P][Q];
   if (apq != 0.0f) {
-    const float theta = (S[Q][Q] - S[P][P]) / (2.0f * apq);
+    // Rotation angle (Rutishauser): t = tan(angle).  Approximate division and
+    // square root suffice here: c and s below are renormalised, so U and V
+    // stay orthogonal, and the next sweep removes the residual off-diagonal.
+    const float theta = __fdividef(S[Q][Q] - S[P][P], 2.0f * apq);
     const float at = fabsf(theta);
     float t;
     if (at > 1e15f) {
-      t = 0.5f / theta;
+      t = __fdividef(0.5f, theta);
     } else {
-      t = 1.0f / (at + sqrtf(fmaf(theta, theta, 1.0f)));
+      const float r = fmaf(theta, theta, 1.0f);
+      t = __fdividef(1.0f, at + r * rsqrtf(r));
       t = theta < 0.0f ? -t : t;
     }
     const float c = rsqrt_nr(fmaf(t, t, 1.0f));
@@ -97,6 +101,46 @@ __device__ __forceinline__ void cond_swap(bool doit, float (&B)[3][3], float (&V
   const float ri = rho[I], rj = rho[J];
   rho[I] = doit ? rj : ri;
   rho[J] = doit ? ri : rj;
+}
+
+// Rotation factor R of the polar decomposition F = R S by Newton's
+// iteration R <- (R + R^{-T}) / 2 (Higham, "Computing the polar
+// decomposition - with applications", 1986), starting from R = F.  Valid for
+// det F > 0, where R equals U V^T of the SVD convention above.  Returns false
+// when the last step still moved R by more than `tol` (very large stretch), in
+// which case the caller uses the SVD.
+template <int ITERS = 5>
+__device__ __forceinline__ bool polar_rotation(const float (&F)[3][3], float (&R)[3][3], float tol = 2e-6f) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) R[i][j] = F[i][j];
+  float change = 0.0f;
+#pragma unroll
+  for (int it = 0; it < ITERS; ++it) {
+    float Cf[3][3];  // cofactor matrix: R^{-T} = Cf / det
+    Cf[0][0] = R[1][1] * R[2][2] - R[1][2] * R[2][1];
+    Cf[0][1] = R[1][2] * R[2][0] - R[1][0] * R[2][2];
+    Cf[0][2] = R[1][0] * R[2][1] - R[1][1] * R[2][0];
+    Cf[1][0] = R[0][2] * R[2][1] - R[0][1] * R[2][2];
+    Cf[1][1] = R[0][0] * R[2][2] - R[0][2] * R[2][0];
+    Cf[1][2] = R[0][1] * R[2][0] - R[0][0] * R[2][1];
+    Cf[2][0] = R[0][1] * R[1][2] - R[0][2] * R[1][1];
+    Cf[2][1] = R[0][2] * R[1][0] - R[0][0] * R[1][2];
+    Cf[2][2] = R[0][0] * R[1][1] - R[0][1] * R[1][0];
+    const float det = R[0][0] * Cf[0][0] + R[0][1] * Cf[0][1] + R[0][2] * Cf[0][2];
+    const float h = 0.5f / det;
+    change = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const float r = fmaf(0.5f, R[i][j], h * Cf[i][j]);
+        change = fmaxf(change, fabsf(r - R[i][j]));
+        R[i][j] = r;
+      }
+  }
+  return change <= tol;
 }
 
 template <int SWEEPS = 4>

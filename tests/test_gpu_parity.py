@@ -250,3 +250,35 @@ def test_per_particle_E_matches_oracle():
         s.substep(dt)
     g = s.full_state()['x'].cpu().numpy()
     assert np.linalg.norm(g - R.P.x) / np.linalg.norm(R.P.x) < 1e-4
+
+
+@pytest.mark.parametrize("name", ["mixed_32", "walls_24"])
+def test_golden_fixture_one_substep(name):
+    """One substep from the committed fixture state (all five materials,
+    colliders, walls) against the fixture's float64 outputs; the bound is
+    calibrated by the float32 oracle's own error on the same state."""
+    import json
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", f"{name}.npz"))
+    pp = json.loads(str(g["postprocess"]))
+    s = MPMSolver(tuple(int(r) for r in g["res"]))
+    for c in pp[1:]:
+        if c["kind"] == 0:
+            s.add_surface_collider(c["point"], c["normal"], c.get("surface", 0), c.get("friction", 0.0))
+        else:
+            s.add_sphere_collider(c["point"], c["radius"], c.get("surface", 0))
+    n = g["x"].shape[0]
+    t = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float32)
+    s.load_state_dict(dict(x=t(g["x"]), v=t(g["v"]), C=t(g["C"]), F=t(g["F"]), Jp=t(g["Jp"]),
+                           material=torch.as_tensor(g["material"]), color=torch.zeros(n, dtype=torch.int32)))
+    dt = float(g["dt"])
+    s.substep(dt)
+    st = {k: v.cpu().numpy().astype(np.float64) for k, v in s.full_state().items() if k != 'material'}
+    cfg = O.Config(res=tuple(g["res"]), postprocess=pp)
+    P32 = O.Particles(*(g[k].astype(np.float32) for k in ("x", "v", "C", "F", "Jp")), g["material"].copy())
+    O.substep(cfg, P32, dt)
+    vs = np.abs(g["out_v"]).max()
+    for f, scale in (("x", 1.0), ("v", vs), ("F", 1.0), ("Jp", 1.0), ("C", 4 * cfg.inv_dx * vs)):
+        eg = np.abs(st[f] - g["out_" + f]).max() / scale
+        e32 = np.abs(getattr(P32, f) - g["out_" + f]).max() / scale
+        assert eg <= max(1e-6, 4 * e32), f"{f}: gpu {eg:.3g} f32 oracle {e32:.3g}"

@@ -138,6 +138,30 @@ int mpm_g2p(const MpmParams *p, void *ws, int64_t cap, int64_t n, float *nxt, fl
 int mpm_substep(const MpmParams *p, void *ws, int64_t cap, int64_t n, const float *cur, float *nxt,
                 float dt, float *maxv_out, void *stream);
 
+/* One substep that allocates nothing and needs no caller-provided workspace.
+ * No counterpart in the reference: it exists for callers that cannot call
+ * cudaMalloc (or a caching allocator) at the point they step the simulation,
+ * for example code running inside someone else's stream capture or memory
+ * pool, or a host application that hands the engine only its particle
+ * buffers.  All scratch (binning tables, grids, status) lives in one static
+ * device array of the library, 16 MiB, which every GPU that loads the library
+ * holds until the process exits.
+ *   - The caller passes `cur` and `nxt` (pstate layout, row stride `cap`);
+ *     `nxt` receives the state sorted by grid block, as with mpm_substep.
+ *   - Limits: at most 65,536 particles, and a grid window whose workspace
+ *     fits 16 MiB (about 4,000 blocks of 4^3 nodes, e.g. a 48^3 grid with the
+ *     solver's default margins).  Larger inputs return MPM_E_CAPACITY before
+ *     any device work.
+ *   - The first call on a device looks up the array's device address; make
+ *     that first call before any stream capture.
+ *   - Every call bins all particles itself and clears the scratch it uses,
+ *     since the array keeps the previous call's contents; calls that overlap
+ *     on the GPU (other streams, other threads) share the array and race.
+ *   - The status word of this scratch is not exposed; check results on the
+ *     host (finite positions) when that matters. */
+int mpm_substep_noalloc(const MpmParams *p, int64_t cap, int64_t n, const float *cur, float *nxt, float dt,
+                        float *maxv_out, void *stream);
+
 /* Copy rows of the sorted state back to original particle order:
  * out[id[j]*ncols + c] = pstate[(row0 + c)*cap + j] for c < ncols.
  * Replaces copy_dynamic_nd / copy_dynamic, engine/mpm_solver.py:1146-1191. */

@@ -98,6 +98,7 @@ SIGNATURES = {
     "mpm_grid_update": [_P, _v, _i64, _f, _v],
     "mpm_g2p": [_P, _v, _i64, _i64, _v, _f, _v, _v],
     "mpm_substep": [_P, _v, _i64, _i64, _v, _v, _f, _v, _v],
+    "mpm_substep_noalloc": [_P, _i64, _i64, _v, _v, _f, _v, _v],
     "mpm_gather_rows": [_v, _i64, _i64, _i32, _i32, _v, _v],
     "mpm_status_ptr": [_P, _v, _i64, ctypes.POINTER(ctypes.c_void_p)],
     "mpm_views": [_P, _v, _i64, ctypes.POINTER(MpmViews)],

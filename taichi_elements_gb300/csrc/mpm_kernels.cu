@@ -642,6 +642,36 @@ static bool params_ok(const MpmParams *p) {
 
 static int last_error() { return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_E_CUDA; }
 
+// ------------------------------------------- allocation-free substep ----
+//
+// Scratch of mpm_substep_noalloc: a file-scope device array, so callers that
+// cannot allocate device memory can still run a substep.  Every device that
+// loads this library keeps these bytes for the life of the process.  Host
+// code must not use `g_static_scratch` as a pointer (on the host it names a
+// stand-in object); its device address is looked up once per device with
+// cudaGetSymbolAddress and passed to the kernels.
+constexpr size_t kStaticScratchBytes = size_t(16) << 20;  // 16 MiB
+constexpr int64_t kStaticMaxParticles = 65536;
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+static void *g_static_addr[64];
+static std::mutex g_static_mu;
+
+// Device address of the static scratch on the current device (set up on the
+// first call per device).
+static int static_scratch_addr(void **out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return MPM_E_CUDA;
+  std::lock_guard<std::mutex> lk(g_static_mu);
+  if (!g_static_addr[dev]) {
+    void *ptr = nullptr;
+    if (cudaGetSymbolAddress(&ptr, g_static_scratch) != cudaSuccess || !ptr) return MPM_E_CUDA;
+    g_static_addr[dev] = ptr;
+  }
+  *out = g_static_addr[dev];
+  return MPM_OK;
+}
+
 }  // namespace mpm
 
 using namespace mpm;
@@ -735,6 +765,41 @@ int mpm_substep(const MpmParams *p, void *ws, int64_t cap, int64_t n, const floa
   rc = mpm_grid_update(p, ws, cap, dt, stream);
   if (rc) return rc;
   return mpm_g2p(p, ws, cap, n, nxt, dt, maxv_out, stream);
+}
+
+int mpm_substep_noalloc(const MpmParams *p, int64_t cap, int64_t n, const float *cur, float *nxt, float dt,
+                        float *maxv_out, void *stream) {
+  if (!params_ok(p) || !cur || !nxt || n < 0 || n > cap) return MPM_E_INVALID;
+  if (n > kStaticMaxParticles) return MPM_E_CAPACITY;
+  const size_t bytes = ws_layout(*p, kStaticMaxParticles, nullptr, nullptr);
+  if (bytes > kStaticScratchBytes) return MPM_E_CAPACITY;
+  const DevInfo *di = dev_info();
+  if (!di) return MPM_E_CUDA;
+  void *base = nullptr;
+  const int rc = static_scratch_addr(&base);
+  if (rc) return rc;
+  Ws w;
+  ws_layout(*p, kStaticMaxParticles, (char *)base, &w);
+  cudaStream_t s = (cudaStream_t)stream;
+  // The scratch keeps whatever the previous call left: zero the counters,
+  // block flags, cell counters and grids this call relies on.
+  if (cudaMemsetAsync(base, 0, bytes, s) != cudaSuccess) return MPM_E_CUDA;
+  if (n > 0) {
+    k_bin_count<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(*p, w, cur, cap, 0, n);
+    k_flags_count<<<w.nflagtiles, 256, 0, s>>>(*p, w);
+    k_flags_write<<<w.nflagtiles, 256, 0, s>>>(*p, w);
+    k_pb_stats<<<w.nstattiles, 256, 0, s>>>(*p, w);
+    k_pb_scan<<<w.nstattiles, 256, 0, s>>>(*p, w);
+    k_pb_levels<<<di->sms * 8, 256, 0, s>>>(*p, w, kStaticMaxParticles);
+    k_scatter<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(*p, w, n);
+    if (p->has_Ep)
+      k_p2g<true><<<di->p2g_ep_ctas, kP2GThreads, 0, s>>>(*p, w, cur, nxt, cap, dt);
+    else
+      k_p2g<false><<<di->p2g_ctas, kP2GThreads, 0, s>>>(*p, w, cur, nxt, cap, dt);
+    k_grid<<<di->sms * 8, 256, 0, s>>>(*p, w, dt);
+    k_g2p<<<di->g2p_ctas, kG2PThreads, 0, s>>>(*p, w, nxt, cap, dt, maxv_out);
+  }
+  return last_error();
 }
 
 int mpm_gather_rows(const float *pstate, int64_t cap, int64_t n, int32_t row0, int32_t ncols, float *out,

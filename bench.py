@@ -243,6 +243,9 @@ def run_gb300(args):
     e2e = None
     if not args.no_e2e:
         e2e = run_e2e(sc, args, ws)
+    batched = None
+    if not args.no_batched:
+        batched = run_batched_measure()
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(sc, args)
@@ -281,6 +284,7 @@ def run_gb300(args):
         "clocks": clk.summary(),
         "e2e": e2e,
         "cpu_baseline": cpu,
+        "batched": batched,
     }
     if rank == 0:
         print(json.dumps(line))
@@ -324,6 +328,51 @@ def run_e2e(sc, args, ws):
             "step": f"one step(frame_dt) frame of {count} substeps + particle_info(); read_restart of the scene "
                     f"from pinned host memory inside the timed region (amortised over {frames} frames)",
             "frames": frames, "seconds": t}
+
+
+def run_batched_measure(frames=3, substeps=50):
+    """64 independent scenes (grids 32-96^3, 8K-300K particles each) advanced
+    by the batched engine in CUDA-graph frames of `substeps` substeps, and the
+    same scenes advanced by the plain solver looped scene by scene."""
+    import torch
+
+    from taichi_elements_gb300 import scenes
+    from taichi_elements_gb300.batched import BatchedMPM, BatchScene
+    raw = scenes.batched_scenes()
+    total = sum(s.n for s in raw)
+    B = BatchedMPM([BatchScene.from_scene(s) for s in raw])
+    stream = torch.cuda.current_stream()
+    for _ in range(2):
+        B.substeps(substeps)  # first run, then graph capture
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(frames):
+        B.substeps(substeps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    B.check_status()
+    t_b = e0.elapsed_time(e1) / 1e3
+    del B
+    solvers = [s.make_solver() for s in raw]
+    for sv, s in zip(solvers, raw):
+        sv._prepare(s.default_dt)
+        for _ in range(2):
+            sv._run_frame(substeps, s.default_dt)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(frames):
+        for sv, s in zip(solvers, raw):
+            sv._run_frame(substeps, s.default_dt)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_l = e0.elapsed_time(e1) / 1e3
+    v_b = total * substeps * frames / t_b
+    v_l = total * substeps * frames / t_l
+    return {"value": v_b, "unit": "particle-substeps/s", "looped_plain_value": v_l, "speedup_vs_looped": v_b / v_l,
+            "scenes": len(raw), "particles": total, "substeps_per_frame": substeps, "frames": frames,
+            "workload": "64 scenes, grids {32,48,64,96}^3, 8K-300K particles in 1-3 cubes, 4 materials, "
+                        "per-scene E log-uniform 1e4-1e6, CUDA-graph 50-substep frames"}
 
 
 def cpu_baseline(sc, args, budget_s=None):
@@ -404,6 +453,7 @@ def main():
     ap.add_argument("--chunk", type=int, default=None)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--e2e-frames", type=int, default=3)
     ap.add_argument("--e2e-substeps", type=int, default=50)

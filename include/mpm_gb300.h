@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define MPM_ABI_VERSION 1
+#define MPM_ABI_VERSION 2
 #define MPM_NROWS 28
 #define MPM_MAX_COLLIDERS 16 /* post-process records, box included */
 
@@ -85,6 +85,16 @@ typedef struct MpmParams {
   float gravity[3];
   float stress_k; /* p_vol * 4 * inv_dx^2            (mpm_solver.py:569) */
   float sand_k;   /* (3 la0 + 2 mu0) / (2 mu0)        (mpm_solver.py:335-337) */
+  /* Batched mode only (zero otherwise).  Scenes live side by side in one
+   * grid window, scene s in slot (s % slots[0], s / slots[0] % slots[1],
+   * s / (slots[0]*slots[1])) of slot_nb blocks per axis.  Each scene's row of
+   * the scene table repeats win_nb/chunk/slots and shifts win_lo so that its
+   * own grid frame maps into its slot; particles carry their scene index in
+   * bits 8..30 of the material word. */
+  int32_t n_scenes;
+  int32_t slot_nb[3];
+  int32_t slots[3];
+  float dt; /* batched mode: this scene's substep dt */
   MpmCollider colliders[MPM_MAX_COLLIDERS];
 } MpmParams;
 
@@ -137,6 +147,22 @@ int mpm_g2p(const MpmParams *p, void *ws, int64_t cap, int64_t n, float *nxt, fl
  * After it returns (on the stream), `nxt` holds the state. */
 int mpm_substep(const MpmParams *p, void *ws, int64_t cap, int64_t n, const float *cur, float *nxt,
                 float dt, float *maxv_out, void *stream);
+
+/* Batched form: bins particles [begin, end) of a multi-scene state.  `p` is
+ * the batch header (window, chunk, slot layout, n_scenes) and `scenes` a
+ * device array of n_scenes per-scene MpmParams rows (see MpmParams).  No
+ * counterpart in the reference, which runs one MPMSolver per scene; this is
+ * build_pid (engine/mpm_solver.py:344-361) for many scenes in one launch. */
+int mpm_batch_bin_count(const MpmParams *p, const MpmParams *scenes, void *ws, int64_t cap, const float *pstate,
+                        int64_t begin, int64_t end, void *stream);
+
+/* Batched substep: one substep of every scene (each with its own dt, E,
+ * gravity, grid resolution and post-process list from its `scenes` row) in
+ * the same kernel launches as a single scene.  maxv_out: device float array
+ * of n_scenes (per-scene max |v|, zeroed by the caller), or NULL.  Replaces a
+ * host loop of engine/mpm_solver.py:789-799 over independent solvers. */
+int mpm_batch_substep(const MpmParams *p, const MpmParams *scenes, void *ws, int64_t cap, int64_t n,
+                      const float *cur, float *nxt, float *maxv_out, void *stream);
 
 /* One substep that allocates nothing and needs no caller-provided workspace.
  * No counterpart in the reference: it exists for callers that cannot call

@@ -12,7 +12,7 @@ from pathlib import Path
 
 from . import build as _build
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 NROWS = 28
 MAX_COLLIDERS = 16
 
@@ -64,6 +64,10 @@ class MpmParams(ctypes.Structure):
         ("gravity", ctypes.c_float * 3),
         ("stress_k", ctypes.c_float),
         ("sand_k", ctypes.c_float),
+        ("n_scenes", ctypes.c_int32),
+        ("slot_nb", ctypes.c_int32 * 3),
+        ("slots", ctypes.c_int32 * 3),
+        ("dt", ctypes.c_float),
         ("colliders", MpmCollider * MAX_COLLIDERS),
     ]
 
@@ -99,6 +103,8 @@ SIGNATURES = {
     "mpm_g2p": [_P, _v, _i64, _i64, _v, _f, _v, _v],
     "mpm_substep": [_P, _v, _i64, _i64, _v, _v, _f, _v, _v],
     "mpm_substep_noalloc": [_P, _i64, _i64, _v, _v, _f, _v, _v],
+    "mpm_batch_bin_count": [_P, _v, _v, _i64, _v, _i64, _i64, _v],
+    "mpm_batch_substep": [_P, _v, _v, _i64, _i64, _v, _v, _v, _v],
     "mpm_gather_rows": [_v, _i64, _i64, _i32, _i32, _v, _v],
     "mpm_status_ptr": [_P, _v, _i64, ctypes.POINTER(ctypes.c_void_p)],
     "mpm_views": [_P, _v, _i64, ctypes.POINTER(MpmViews)],

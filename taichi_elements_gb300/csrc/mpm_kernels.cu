@@ -44,9 +44,43 @@ __device__ __forceinline__ void set_status(const Ws &w, uint32_t bits) {
 // set bits are a subset of `need`.
 __constant__ int kNeighbourMask[8] = {0x01, 0x03, 0x05, 0x0F, 0x11, 0x33, 0x55, 0xFF};
 
-__device__ __forceinline__ void bin_one(const MpmParams &P, const Ws &w, int64_t i, float x0, float x1,
-                                        float x2, uint32_t &bad) {
-  const Base b = particle_base(P, x0, x1, x2, bad);
+// Scene constants.  A single scene uses the kernel's own parameters; in
+// batched mode a particle's scene index sits in bits 8.. of its material word
+// and a grid block's scene follows from its slot in the shared window.
+template <bool BATCH>
+__device__ __forceinline__ const MpmParams &scene_of_particle(const MpmParams &P, const MpmParams *tab, int matword) {
+  if constexpr (BATCH) {
+    const int s = min(max(matword >> 8, 0), P.n_scenes - 1);
+    return tab[s];
+  } else {
+    return P;
+  }
+}
+
+template <bool BATCH>
+__device__ __forceinline__ int scene_index_of_block(const MpmParams &P, int bx, int by, int bz) {
+  if constexpr (BATCH) {
+    const int s = bx / P.slot_nb[0] + P.slots[0] * (by / P.slot_nb[1] + P.slots[1] * (bz / P.slot_nb[2]));
+    return min(max(s, 0), P.n_scenes - 1);
+  } else {
+    return 0;
+  }
+}
+
+template <bool BATCH>
+__device__ __forceinline__ const MpmParams &scene_of_block(const MpmParams &P, const MpmParams *tab, int bx, int by,
+                                                           int bz) {
+  if constexpr (BATCH) {
+    return tab[scene_index_of_block<true>(P, bx, by, bz)];
+  } else {
+    return P;
+  }
+}
+
+template <bool BATCH>
+__device__ __forceinline__ void bin_one(const MpmParams &P, const MpmParams *tab, const Ws &w, int64_t i, float x0,
+                                        float x1, float x2, int matword, uint32_t &bad) {
+  const Base b = particle_base(scene_of_particle<BATCH>(P, tab, matword), x0, x1, x2, bad);
   const int key = cell_key(P, b);
   atomicAdd(&w.cell_cnt[key], 1);  // result unused: a fire-and-forget reduction
   const int blin = key >> 6;
@@ -61,11 +95,15 @@ __device__ __forceinline__ void bin_one(const MpmParams &P, const Ws &w, int64_t
   w.cellkey[i] = key;
 }
 
-__global__ void k_bin_count(const MpmParams P, const Ws w, const float *__restrict__ ps, int64_t cap,
-                            int64_t begin, int64_t end) {
+template <bool BATCH>
+__global__ void k_bin_count(const MpmParams P, const MpmParams *tab, const Ws w, const float *__restrict__ ps,
+                            int64_t cap, int64_t begin, int64_t end) {
   const int64_t i = begin + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t bad = 0;
-  if (i < end) bin_one(P, w, i, ps[kX * cap + i], ps[(kX + 1) * cap + i], ps[(kX + 2) * cap + i], bad);
+  if (i < end) {
+    const int matword = BATCH ? __float_as_int(ps[kMat * cap + i]) : 0;
+    bin_one<BATCH>(P, tab, w, i, ps[kX * cap + i], ps[(kX + 1) * cap + i], ps[(kX + 2) * cap + i], matword, bad);
+  }
   set_status(w, bad);
 }
 
@@ -332,8 +370,8 @@ __device__ __forceinline__ float4 f4add(float4 a, float4 b) {
   return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
 }
 
-template <bool HAS_EP>
-__global__ __launch_bounds__(kP2GThreads, 5) void k_p2g(const MpmParams P, const Ws w,
+template <bool HAS_EP, bool BATCH>
+__global__ __launch_bounds__(kP2GThreads, 5) void k_p2g(const MpmParams P, const MpmParams *tab, const Ws w,
                                                        const float *__restrict__ cur,
                                                        float *__restrict__ nxt, int64_t cap, float dt) {
   __shared__ float4 tiles[kP2GWarps][kTileN];
@@ -362,37 +400,39 @@ __global__ __launch_bounds__(kP2GThreads, 5) void k_p2g(const MpmParams P, const
       float wt[3][3];
       int lx = 0, ly = 0, lz = 0;
       if (active) {
+        const float *src = cur + i;
+        float *dst = nxt + j;
         float x[3], v[3], C[3][3], F[3][3];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          x[d] = cur[(kX + d) * cap + i];
-          v[d] = cur[(kV + d) * cap + i];
-        }
+        for (int d = 0; d < 3; ++d) x[d] = src[(kX + d) * cap];
+        const int matword = __float_as_int(src[kMat * cap]);
+        const int mat = matword & 0xFF;
+        const MpmParams &S = scene_of_particle<BATCH>(P, tab, matword);
+        const float Ep = HAS_EP ? src[kEp * cap] : 0.0f;
+        // carried fields go to the sorted position j right away
+#pragma unroll
+        for (int d = 0; d < 3; ++d) dst[(kX + d) * cap] = x[d];
+        dst[kMat * cap] = __int_as_float(matword);
+        dst[kId * cap] = src[kId * cap];
+        if (HAS_EP) dst[kEp * cap] = Ep;
+        const Base b = particle_base(S, x[0], x[1], x[2], bad);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) v[d] = src[(kV + d) * cap];
 #pragma unroll
         for (int a = 0; a < 9; ++a) {
-          C[a / 3][a % 3] = cur[(kC + a) * cap + i];
-          F[a / 3][a % 3] = cur[(kF + a) * cap + i];
+          C[a / 3][a % 3] = src[(kC + a) * cap];
+          F[a / 3][a % 3] = src[(kF + a) * cap];
         }
-        float Jp = cur[kJp * cap + i];
-        const int mat = __float_as_int(cur[kMat * cap + i]);
-        const float idf = cur[kId * cap + i];
-        const float Ep = HAS_EP ? cur[kEp * cap + i] : 0.0f;
-        const Base b = particle_base(P, x[0], x[1], x[2], bad);
-        const P2GOut o = constitutive(P, dt, mat, Ep, F, Jp, C);
-        // carried fields, sorted position j
+        float Jp = src[kJp * cap];
+        const P2GOut o = constitutive(S, BATCH ? S.dt : dt, mat, Ep, F, Jp, C);
 #pragma unroll
-        for (int d = 0; d < 3; ++d) nxt[(kX + d) * cap + j] = x[d];
-#pragma unroll
-        for (int a = 0; a < 9; ++a) nxt[(kF + a) * cap + j] = F[a / 3][a % 3];
-        nxt[kJp * cap + j] = Jp;
-        nxt[kMat * cap + j] = __int_as_float(mat);
-        nxt[kId * cap + j] = idf;
-        if (HAS_EP) nxt[kEp * cap + j] = Ep;
+        for (int a = 0; a < 9; ++a) dst[(kF + a) * cap] = F[a / 3][a % 3];
+        dst[kJp * cap] = Jp;
         if (mat == 4) {  // stationary: G2P keeps v and C (:722)
 #pragma unroll
-          for (int d = 0; d < 3; ++d) nxt[(kV + d) * cap + j] = v[d];
+          for (int d = 0; d < 3; ++d) dst[(kV + d) * cap] = v[d];
 #pragma unroll
-          for (int a = 0; a < 9; ++a) nxt[(kC + a) * cap + j] = C[a / 3][a % 3];
+          for (int a = 0; a < 9; ++a) dst[(kC + a) * cap] = C[a / 3][a % 3];
         }
         lx = b.b[0] - bx * 4;
         ly = b.b[1] - by * 4;
@@ -408,11 +448,11 @@ __global__ __launch_bounds__(kP2GThreads, 5) void k_p2g(const MpmParams P, const
 #pragma unroll
           for (int d = 0; d < 3; ++d)
             q[d] = o.mass * v[d] -
-                   P.dx * (o.affine[d][0] * b.fx[0] + o.affine[d][1] * b.fx[1] + o.affine[d][2] * b.fx[2]);
+                   S.dx * (o.affine[d][0] * b.fx[0] + o.affine[d][1] * b.fx[1] + o.affine[d][2] * b.fx[2]);
 #pragma unroll
           for (int r = 0; r < 3; ++r)
 #pragma unroll
-            for (int c = 0; c < 3; ++c) adx[r][c] = o.affine[r][c] * P.dx;
+            for (int c = 0; c < 3; ++c) adx[r][c] = o.affine[r][c] * S.dx;
         }
       }
       // lanes sharing a cell scatter in successive rounds
@@ -466,7 +506,8 @@ __global__ __launch_bounds__(kP2GThreads, 5) void k_p2g(const MpmParams P, const
 
 // --------------------------------------------------------------- grid ----
 
-__global__ __launch_bounds__(256) void k_grid(const MpmParams P, const Ws w, float dt) {
+template <bool BATCH>
+__global__ __launch_bounds__(256) void k_grid(const MpmParams P, const MpmParams *tab, const Ws w, float dt) {
   const int ng = w.counters[1];
   const int64_t total = (int64_t)ng * kBlockCells;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
@@ -478,22 +519,24 @@ __global__ __launch_bounds__(256) void k_grid(const MpmParams P, const Ws w, flo
     w.grid_mom[addr] = make_float4(0.f, 0.f, 0.f, 0.f);
     int bx, by, bz;
     block_coords(P, blin, bx, by, bz);
-    const int I[3] = {P.win_lo[0] + bx * 4 + (l >> 4), P.win_lo[1] + by * 4 + ((l >> 2) & 3),
-                      P.win_lo[2] + bz * 4 + (l & 3)};
-    const float3 v = grid_node_update(P, I, g.x, make_float3(g.y, g.z, g.w), dt);
+    const MpmParams &S = scene_of_block<BATCH>(P, tab, bx, by, bz);
+    const int I[3] = {S.win_lo[0] + bx * 4 + (l >> 4), S.win_lo[1] + by * 4 + ((l >> 2) & 3),
+                      S.win_lo[2] + bz * 4 + (l & 3)};
+    const float3 v = grid_node_update(S, I, g.x, make_float3(g.y, g.z, g.w), BATCH ? S.dt : dt);
     w.grid_vel[addr] = make_float4(v.x, v.y, v.z, g.x);
   }
 }
 
 // ---------------------------------------------------------------- G2P ----
 
-__global__ __launch_bounds__(kG2PThreads, 8) void k_g2p(const MpmParams P, const Ws w, float *__restrict__ st,
-                                                       int64_t cap, float dt, float *maxv_out) {
+template <bool BATCH>
+__global__ __launch_bounds__(kG2PThreads, 8) void k_g2p(const MpmParams P, const MpmParams *tab, const Ws w,
+                                                       float *__restrict__ st, int64_t cap, float dt,
+                                                       float *maxv_out) {
   __shared__ float4 vt[kTileN];
   const int nitems = (int)min((int64_t)w.counters[2], w.items_cap);
   uint32_t bad = 0;
   float vmax = 0.0f;
-  const float s4 = 4.0f * P.inv_dx;
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const int2 item = w.items[it];
     const int k = item.x, start = item.y;
@@ -513,8 +556,12 @@ __global__ __launch_bounds__(kG2PThreads, 8) void k_g2p(const MpmParams P, const
       float x[3];
 #pragma unroll
       for (int d = 0; d < 3; ++d) x[d] = st[(kX + d) * cap + j];
-      const int mat = __float_as_int(st[kMat * cap + j]);
-      const Base b = particle_base(P, x[0], x[1], x[2], bad);
+      const int matword = __float_as_int(st[kMat * cap + j]);
+      const int mat = matword & 0xFF;
+      const MpmParams &S = scene_of_particle<BATCH>(P, tab, matword);
+      const float s4 = 4.0f * S.inv_dx;
+      const float dts = BATCH ? S.dt : dt;
+      const Base b = particle_base(S, x[0], x[1], x[2], bad);
       float wt[3][3];
       bspline_weights(b.fx, wt);
       const int lx = b.b[0] - bx * 4, ly = b.b[1] - by * 4, lz = b.b[2] - bz * 4;
@@ -566,7 +613,7 @@ __global__ __launch_bounds__(kG2PThreads, 8) void k_g2p(const MpmParams P, const
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
           vv[d] = nv[d];
-          x[d] = x[d] + dt * nv[d];
+          x[d] = x[d] + dts * nv[d];
           st[(kV + d) * cap + j] = nv[d];
           st[(kX + d) * cap + j] = x[d];
         }
@@ -577,12 +624,19 @@ __global__ __launch_bounds__(kG2PThreads, 8) void k_g2p(const MpmParams P, const
         for (int d = 0; d < 3; ++d) vv[d] = st[(kV + d) * cap + j];
       }
       vmax = fmaxf(vmax, fmaxf(fabsf(vv[0]), fmaxf(fabsf(vv[1]), fabsf(vv[2]))));
-      bin_one(P, w, j, x[0], x[1], x[2], bad);  // next substep's build_pid
+      bin_one<BATCH>(P, tab, w, j, x[0], x[1], x[2], matword, bad);  // next substep's build_pid
+    }
+    if (BATCH && maxv_out) {  // per-scene maximum, flushed per work item
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+      if ((threadIdx.x & 31) == 0 && vmax > 0.0f)
+        atomicMax((int *)&maxv_out[scene_index_of_block<BATCH>(P, bx, by, bz)], __float_as_int(vmax));
+      vmax = 0.0f;
     }
     __syncthreads();
   }
   set_status(w, bad);
-  if (maxv_out) {
+  if (!BATCH && maxv_out) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
     if ((threadIdx.x & 31) == 0 && vmax > 0.0f) atomicMax((int *)maxv_out, __float_as_int(vmax));
@@ -603,6 +657,7 @@ __global__ void k_gather_rows(const float *__restrict__ ps, int64_t cap, int64_t
 struct DevInfo {
   int sms = 0;
   int p2g_ctas = 0, p2g_ep_ctas = 0, g2p_ctas = 0;
+  int p2g_b_ctas = 0, p2g_ep_b_ctas = 0, g2p_b_ctas = 0;
 };
 
 static DevInfo g_dev[64];
@@ -616,13 +671,19 @@ static const DevInfo *dev_info() {
   if (d.sms == 0) {
     int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return nullptr;
-    int a = 0, b = 0, c = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_p2g<false>, kP2GThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_p2g<true>, kP2GThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_g2p, kG2PThreads, 0);
+    int a = 0, b = 0, c = 0, a2 = 0, b2 = 0, c2 = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_p2g<false, false>, kP2GThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_p2g<true, false>, kP2GThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_g2p<false>, kG2PThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a2, k_p2g<false, true>, kP2GThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_p2g<true, true>, kP2GThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c2, k_g2p<true>, kG2PThreads, 0);
     d.p2g_ctas = sms * (a > 0 ? a : 1);
     d.p2g_ep_ctas = sms * (b > 0 ? b : 1);
     d.g2p_ctas = sms * (c > 0 ? c : 1);
+    d.p2g_b_ctas = sms * (a2 > 0 ? a2 : 1);
+    d.p2g_ep_b_ctas = sms * (b2 > 0 ? b2 : 1);
+    d.g2p_b_ctas = sms * (c2 > 0 ? c2 : 1);
     d.sms = sms;
   }
   return &d;
@@ -700,7 +761,8 @@ int mpm_bin_count(const MpmParams *p, void *ws, int64_t cap, const float *pstate
   Ws w;
   ws_layout(*p, cap, (char *)ws, &w);
   const int64_t n = end - begin;
-  k_bin_count<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(*p, w, pstate, cap, begin, end);
+  k_bin_count<false><<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(*p, nullptr, w, pstate, cap, begin,
+                                                                                   end);
   return last_error();
 }
 
@@ -729,9 +791,9 @@ int mpm_p2g(const MpmParams *p, void *ws, int64_t cap, int64_t n, const float *c
   ws_layout(*p, cap, (char *)ws, &w);
   cudaStream_t s = (cudaStream_t)stream;
   if (p->has_Ep)
-    k_p2g<true><<<di->p2g_ep_ctas, kP2GThreads, 0, s>>>(*p, w, cur, nxt, cap, dt);
+    k_p2g<true, false><<<di->p2g_ep_ctas, kP2GThreads, 0, s>>>(*p, nullptr, w, cur, nxt, cap, dt);
   else
-    k_p2g<false><<<di->p2g_ctas, kP2GThreads, 0, s>>>(*p, w, cur, nxt, cap, dt);
+    k_p2g<false, false><<<di->p2g_ctas, kP2GThreads, 0, s>>>(*p, nullptr, w, cur, nxt, cap, dt);
   return last_error();
 }
 
@@ -741,7 +803,7 @@ int mpm_grid_update(const MpmParams *p, void *ws, int64_t cap, float dt, void *s
   if (!di) return MPM_E_CUDA;
   Ws w;
   ws_layout(*p, cap, (char *)ws, &w);
-  k_grid<<<di->sms * 8, 256, 0, (cudaStream_t)stream>>>(*p, w, dt);
+  k_grid<false><<<di->sms * 8, 256, 0, (cudaStream_t)stream>>>(*p, nullptr, w, dt);
   return last_error();
 }
 
@@ -752,7 +814,7 @@ int mpm_g2p(const MpmParams *p, void *ws, int64_t cap, int64_t n, float *nxt, fl
   if (!di) return MPM_E_CUDA;
   Ws w;
   ws_layout(*p, cap, (char *)ws, &w);
-  k_g2p<<<di->g2p_ctas, kG2PThreads, 0, (cudaStream_t)stream>>>(*p, w, nxt, cap, dt, maxv_out);
+  k_g2p<false><<<di->g2p_ctas, kG2PThreads, 0, (cudaStream_t)stream>>>(*p, nullptr, w, nxt, cap, dt, maxv_out);
   return last_error();
 }
 
@@ -765,6 +827,48 @@ int mpm_substep(const MpmParams *p, void *ws, int64_t cap, int64_t n, const floa
   rc = mpm_grid_update(p, ws, cap, dt, stream);
   if (rc) return rc;
   return mpm_g2p(p, ws, cap, n, nxt, dt, maxv_out, stream);
+}
+
+static bool batch_ok(const MpmParams *p) {
+  if (!params_ok(p) || p->n_scenes < 1) return false;
+  int64_t slots = 1;
+  for (int d = 0; d < 3; ++d) {
+    if (p->slot_nb[d] <= 0 || p->slots[d] <= 0) return false;
+    if ((int64_t)p->slot_nb[d] * p->slots[d] > p->win_nb[d]) return false;
+    slots *= p->slots[d];
+  }
+  return slots >= p->n_scenes;
+}
+
+int mpm_batch_bin_count(const MpmParams *p, const MpmParams *scenes, void *ws, int64_t cap, const float *pstate,
+                        int64_t begin, int64_t end, void *stream) {
+  if (!batch_ok(p) || !scenes || !ws || !pstate || begin < 0 || end > cap || begin > end) return MPM_E_INVALID;
+  if (end == begin) return MPM_OK;
+  Ws w;
+  ws_layout(*p, cap, (char *)ws, &w);
+  const int64_t n = end - begin;
+  k_bin_count<true><<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(*p, scenes, w, pstate, cap, begin,
+                                                                                  end);
+  return last_error();
+}
+
+int mpm_batch_substep(const MpmParams *p, const MpmParams *scenes, void *ws, int64_t cap, int64_t n,
+                      const float *cur, float *nxt, float *maxv_out, void *stream) {
+  if (!batch_ok(p) || !scenes || !ws || !cur || !nxt || n < 0 || n > cap) return MPM_E_INVALID;
+  int rc = mpm_bin_finalize(p, ws, cap, n, stream);
+  if (rc) return rc;
+  const DevInfo *di = dev_info();
+  if (!di) return MPM_E_CUDA;
+  Ws w;
+  ws_layout(*p, cap, (char *)ws, &w);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (p->has_Ep)
+    k_p2g<true, true><<<di->p2g_ep_b_ctas, kP2GThreads, 0, s>>>(*p, scenes, w, cur, nxt, cap, 0.0f);
+  else
+    k_p2g<false, true><<<di->p2g_b_ctas, kP2GThreads, 0, s>>>(*p, scenes, w, cur, nxt, cap, 0.0f);
+  k_grid<true><<<di->sms * 8, 256, 0, s>>>(*p, scenes, w, 0.0f);
+  k_g2p<true><<<di->g2p_b_ctas, kG2PThreads, 0, s>>>(*p, scenes, w, nxt, cap, 0.0f, maxv_out);
+  return last_error();
 }
 
 int mpm_substep_noalloc(const MpmParams *p, int64_t cap, int64_t n, const float *cur, float *nxt, float dt,
@@ -785,7 +889,7 @@ int mpm_substep_noalloc(const MpmParams *p, int64_t cap, int64_t n, const float 
   // block flags, cell counters and grids this call relies on.
   if (cudaMemsetAsync(base, 0, bytes, s) != cudaSuccess) return MPM_E_CUDA;
   if (n > 0) {
-    k_bin_count<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(*p, w, cur, cap, 0, n);
+    k_bin_count<false><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(*p, nullptr, w, cur, cap, 0, n);
     k_flags_count<<<w.nflagtiles, 256, 0, s>>>(*p, w);
     k_flags_write<<<w.nflagtiles, 256, 0, s>>>(*p, w);
     k_pb_stats<<<w.nstattiles, 256, 0, s>>>(*p, w);
@@ -793,11 +897,11 @@ int mpm_substep_noalloc(const MpmParams *p, int64_t cap, int64_t n, const float 
     k_pb_levels<<<di->sms * 8, 256, 0, s>>>(*p, w, kStaticMaxParticles);
     k_scatter<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(*p, w, n);
     if (p->has_Ep)
-      k_p2g<true><<<di->p2g_ep_ctas, kP2GThreads, 0, s>>>(*p, w, cur, nxt, cap, dt);
+      k_p2g<true, false><<<di->p2g_ep_ctas, kP2GThreads, 0, s>>>(*p, nullptr, w, cur, nxt, cap, dt);
     else
-      k_p2g<false><<<di->p2g_ctas, kP2GThreads, 0, s>>>(*p, w, cur, nxt, cap, dt);
-    k_grid<<<di->sms * 8, 256, 0, s>>>(*p, w, dt);
-    k_g2p<<<di->g2p_ctas, kG2PThreads, 0, s>>>(*p, w, nxt, cap, dt, maxv_out);
+      k_p2g<false, false><<<di->p2g_ctas, kP2GThreads, 0, s>>>(*p, nullptr, w, cur, nxt, cap, dt);
+    k_grid<false><<<di->sms * 8, 256, 0, s>>>(*p, nullptr, w, dt);
+    k_g2p<false><<<di->g2p_ctas, kG2PThreads, 0, s>>>(*p, nullptr, w, nxt, cap, dt, maxv_out);
   }
   return last_error();
 }

@@ -639,7 +639,7 @@ class MPMSolver:
         data = {
             'position': self._gather(ROW_X, 3).cpu().numpy(),
             'velocity': self._gather(ROW_V, 3).cpu().numpy(),
-            'material': self._gather(ROW_MAT, 1).view(torch.int32).reshape(n).cpu().numpy(),
+            'material': (self._gather(ROW_MAT, 1).view(torch.int32).reshape(n) & 0xFF).cpu().numpy(),
             'color': self._color[:n].cpu().numpy() if n else np.zeros(0, np.int32),
         }
         if self.use_emitter_id:
@@ -657,7 +657,7 @@ class MPMSolver:
             'C': g[:, ROW_C:ROW_C + 9].reshape(n, 3, 3),
             'F': g[:, ROW_F:ROW_F + 9].reshape(n, 3, 3),
             'Jp': g[:, ROW_JP],
-            'material': g[:, ROW_MAT].contiguous().view(torch.int32),
+            'material': g[:, ROW_MAT].contiguous().view(torch.int32) & 0xFF,
         }
 
     def state_dict(self):

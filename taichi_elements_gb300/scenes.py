@@ -138,7 +138,9 @@ def batched_scenes(seed: int = 4, n_scenes: int = 64):
     """64 independent scenes: grid res from {32,48,64,96}^3, particle counts
     log-uniform in [8K, 300K] over 1-3 random cubes at 8 particles per cell,
     material per cube uniform over water/elastic/snow/sand, per-scene E
-    log-uniform in [1e4, 1e6]; 50-substep frames."""
+    log-uniform in [1e4, 1e6]; 50-substep frames.  A cube that would not fit
+    inside the box at 8 particles per cell (large counts on coarse grids) is
+    shrunk to fit, which raises its particle density."""
     rng = np.random.default_rng(seed)
     out = []
     for s in range(n_scenes):
@@ -151,9 +153,10 @@ def batched_scenes(seed: int = 4, n_scenes: int = 64):
         xs, ms = [], []
         for j in range(k):
             m = int(split[j])
+            margin = 3 * dx + 0.01
             side = (m / 8.0)**(1.0 / 3.0) * dx
-            side = min(side, 0.8)
-            lo = rng.uniform(3 * dx + 0.01, 1 - 3 * dx - 0.01 - side, 3)
+            side = min(side, 1 - 2 * margin - 0.02)
+            lo = rng.uniform(margin, 1 - margin - side, 3)
             xs.append(_cube(rng, lo, side, m))
             ms.append(np.full(m, int(rng.integers(0, 4)), np.int32))
         x = np.concatenate(xs)

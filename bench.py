@@ -246,6 +246,9 @@ def run_gb300(args):
     batched = None
     if not args.no_batched:
         batched = run_batched_measure()
+    adjoint = None
+    if not args.no_adjoint:
+        adjoint = run_adjoint_measure()
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(sc, args)
@@ -285,6 +288,7 @@ def run_gb300(args):
         "e2e": e2e,
         "cpu_baseline": cpu,
         "batched": batched,
+        "fwd_adjoint": adjoint,
     }
     if rank == 0:
         print(json.dumps(line))
@@ -375,6 +379,55 @@ def run_batched_measure(frames=3, substeps=50):
                         "per-scene E log-uniform 1e4-1e6, CUDA-graph 50-substep frames"}
 
 
+def run_adjoint_measure(n_substeps=2000, checkpoint_every=50):
+    """Differentiable workload: a 64^3 grid with an elastic cube of 100K
+    particles on a 100K-particle water slab, per-particle E, 2000 substeps,
+    checkpoints every 50.  Times the plain forward rollout and the forward
+    (with checkpoints) plus the hand-written adjoint of a centre-of-mass loss
+    with respect to initial velocities and E."""
+    import torch
+
+    from oracle.torch_ref import com_loss  # loss definition only
+    from taichi_elements_gb300 import scenes
+    from taichi_elements_gb300.differentiable import Rollout, rollout_positions
+    from taichi_elements_gb300.mpm_solver import MPMSolver
+    sc = scenes.elastic_on_water()
+    rng = np.random.default_rng(5)
+    E = np.full(sc.n, 1e6, np.float32) * np.exp(rng.uniform(-0.5, 0.5, sc.n)).astype(np.float32)
+    s = MPMSolver(sc.res, per_particle_E=True)
+    for m in (0, 1):
+        sel = sc.material == m
+        s.add_particles(sc.x[sel], m, E=torch.as_tensor(E[sel]))
+    R = Rollout(s, n_substeps, checkpoint_every=checkpoint_every)
+    v0 = torch.zeros((sc.n, 3), device="cuda")
+    e = torch.tensor(np.concatenate([E[sc.material == m] for m in (0, 1)]), device="cuda")
+    mat = torch.tensor(np.concatenate([sc.material[sc.material == m] for m in (0, 1)]), device="cuda")
+    target = torch.tensor(sc.target, dtype=torch.float32, device="cuda")
+    init = R.initial_state(v0, e)
+    R._run(init, 20)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    R._run(init, n_substeps)
+    torch.cuda.synchronize()
+    t_fwd = time.perf_counter() - t0
+    v = v0.clone().requires_grad_(True)
+    ee = e.clone().requires_grad_(True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    x = rollout_positions(R, v, ee)
+    L = com_loss(x, mat, target)
+    L.backward()
+    torch.cuda.synchronize()
+    t_all = time.perf_counter() - t0
+    return {"value": sc.n * n_substeps / t_all, "unit": "particle-substeps/s (forward+adjoint)",
+            "plain_forward_value": sc.n * n_substeps / t_fwd, "fwd_adjoint_over_forward": t_all / t_fwd,
+            "particles": sc.n, "substeps": n_substeps, "checkpoint_every": checkpoint_every,
+            "seconds_forward": t_fwd, "seconds_forward_adjoint": t_all,
+            "grad_norms": {"v0": float(v.grad.norm()), "E": float(ee.grad.norm())},
+            "workload": "64^3 grid, elastic cube 100K on water slab 100K, per-particle E, f32, "
+                        "loss |com_elastic(T) - target|^2"}
+
+
 def cpu_baseline(sc, args, budget_s=None):
     """The oracle port (C/OpenMP float32, every host thread) on a bounded
     sample: whole-scene substeps until the time budget is used."""
@@ -454,6 +507,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--e2e-frames", type=int, default=3)
     ap.add_argument("--e2e-substeps", type=int, default=50)

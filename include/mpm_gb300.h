@@ -42,6 +42,7 @@ extern "C" {
 #define MPM_STATUS_OUT_OF_GRID 1u  /* a stencil left the grid window (clamped) */
 #define MPM_STATUS_NONFINITE 2u    /* NaN/Inf particle position */
 #define MPM_STATUS_TABLE_OVERFLOW 4u
+#define MPM_STATUS_UNSUPPORTED 8u     /* adjoint met a material it does not differentiate */
 
 /* error codes */
 #define MPM_OK 0
@@ -163,6 +164,30 @@ int mpm_batch_bin_count(const MpmParams *p, const MpmParams *scenes, void *ws, i
  * host loop of engine/mpm_solver.py:789-799 over independent solvers. */
 int mpm_batch_substep(const MpmParams *p, const MpmParams *scenes, void *ws, int64_t cap, int64_t n,
                       const float *cur, float *nxt, float *maxv_out, void *stream);
+
+/* ---- Adjoint of one substep (water and elastic) ----------------------
+ * No counterpart in the reference, which has no autodiff.  Gradient buffers
+ * `gin` / `gout` have 25 float32 rows of `cap` elements indexed by ORIGINAL
+ * particle id: dL/dx (rows 0-2), dL/dv (3-5), dL/dC (6-14), dL/dF (15-23),
+ * dL/dJp (24); `gin` holds the gradient with respect to the state after
+ * substep t, `gout` receives the one before it.  `gE` (float[cap], by id)
+ * accumulates dL/dE for per-particle Young's modulus.  `keep` and `ggrid`
+ * are float4 arrays shaped like the workspace grid (see mpm_workspace_bytes:
+ * window blocks * 64 nodes).
+ * Sequence for substep t, after re-running its forward (bin, finalize, p2g)
+ * from the state before it (`cur`) into `st`:
+ *   mpm_grid_snapshot(keep)      - between mpm_p2g and mpm_grid_update
+ *   mpm_grid_update
+ *   zero ggrid; mpm_g2p_adj      - writes gout rows 0-2, scatters dL/dv_grid
+ *   mpm_grid_adj                 - dL/dv_grid -> dL/d(m, mv) in place
+ *   mpm_p2g_adj                  - adds to gout rows 0-2, writes rows 3-24 */
+int mpm_grid_snapshot(const MpmParams *p, void *ws, int64_t cap, float *keep, void *stream);
+int mpm_g2p_adj(const MpmParams *p, void *ws, int64_t cap, int64_t n, const float *st, float dt, const float *gin,
+                float *gout, float *ggrid, void *stream);
+int mpm_grid_adj(const MpmParams *p, void *ws, int64_t cap, const float *keep, float *ggrid, float dt,
+                 void *stream);
+int mpm_p2g_adj(const MpmParams *p, void *ws, int64_t cap, int64_t n, const float *cur, const float *st, float dt,
+                const float *gin, float *gout, const float *ggrid, float *gE, void *stream);
 
 /* One substep that allocates nothing and needs no caller-provided workspace.
  * No counterpart in the reference: it exists for callers that cannot call

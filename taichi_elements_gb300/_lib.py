@@ -19,6 +19,7 @@ MAX_COLLIDERS = 16
 STATUS_OUT_OF_GRID = 1
 STATUS_NONFINITE = 2
 STATUS_TABLE_OVERFLOW = 4
+STATUS_UNSUPPORTED = 8
 
 # Row indices of the particle-state buffer.
 ROW_X, ROW_V, ROW_C, ROW_F, ROW_JP, ROW_MAT, ROW_ID, ROW_EP = 0, 3, 6, 15, 24, 25, 26, 27
@@ -104,6 +105,10 @@ SIGNATURES = {
     "mpm_substep": [_P, _v, _i64, _i64, _v, _v, _f, _v, _v],
     "mpm_substep_noalloc": [_P, _i64, _i64, _v, _v, _f, _v, _v],
     "mpm_batch_bin_count": [_P, _v, _v, _i64, _v, _i64, _i64, _v],
+    "mpm_grid_snapshot": [_P, _v, _i64, _v, _v],
+    "mpm_g2p_adj": [_P, _v, _i64, _i64, _v, _f, _v, _v, _v, _v],
+    "mpm_grid_adj": [_P, _v, _i64, _v, _v, _f, _v],
+    "mpm_p2g_adj": [_P, _v, _i64, _i64, _v, _v, _f, _v, _v, _v, _v, _v],
     "mpm_batch_substep": [_P, _v, _v, _i64, _i64, _v, _v, _v, _v],
     "mpm_gather_rows": [_v, _i64, _i64, _i32, _i32, _v, _v],
     "mpm_status_ptr": [_P, _v, _i64, ctypes.POINTER(ctypes.c_void_p)],

@@ -127,6 +127,16 @@ __device__ __forceinline__ Base particle_base(const MpmParams &P, float x0, floa
   return r;
 }
 
+__device__ __forceinline__ void set_status(const Ws &w, uint32_t bits) {
+  if (bits) atomicOr((unsigned int *)&w.counters[3], bits);
+}
+
+__device__ __forceinline__ void block_coords(const MpmParams &P, int64_t b, int &bx, int &by, int &bz) {
+  bz = (int)(b % P.win_nb[2]);
+  by = (int)((b / P.win_nb[2]) % P.win_nb[1]);
+  bx = (int)(b / ((int64_t)P.win_nb[1] * P.win_nb[2]));
+}
+
 __device__ __forceinline__ int block_linear(const MpmParams &P, int bx, int by, int bz) {
   return (bx * P.win_nb[1] + by) * P.win_nb[2] + bz;
 }
@@ -341,8 +351,64 @@ done:
   return o;
 }
 
-// Grid node update, engine/mpm_solver.py:586-616 and :618-687.  I is the
-// node's index in the reference grid frame.
+// One grid post-process record applied to a node velocity (the reference's
+// grid_postprocess list, engine/mpm_solver.py:794-795): bounding box
+// (:600-616), surface collider (:647-687) or sphere collider (:618-642).  I is
+// the node's index in the reference grid frame.
+__device__ __forceinline__ void postprocess_op(const MpmParams &P, const MpmCollider &cl, const int (&I)[3],
+                                               float (&v)[3]) {
+  if (cl.kind == 2) {  // bounding box, :600-616
+    const bool unb = cl.surface != 0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const int lo = unb ? -P.grid_size / 2 + P.padding : P.padding;
+      const int hi = unb ? P.grid_size / 2 - P.padding : P.res[d] - P.padding;
+      if (I[d] < lo && v[d] < 0.0f) v[d] = 0.0f;
+      if (I[d] >= hi && v[d] > 0.0f) v[d] = 0.0f;
+    }
+    return;
+  }
+  float off[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) off[d] = (float)I[d] * P.dx - cl.point[d];
+  if (cl.kind == 0) {
+    const float dn = off[0] * cl.normal[0] + off[1] * cl.normal[1] + off[2] * cl.normal[2];
+    if (dn < 0.0f) {
+      if (cl.surface == 0) {
+        v[0] = v[1] = v[2] = 0.0f;
+      } else {
+        const float nc = cl.normal[0] * v[0] + cl.normal[1] * v[1] + cl.normal[2] * v[2];
+        const float s = cl.surface == 1 ? nc : fminf(nc, 0.0f);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) v[d] = v[d] - cl.normal[d] * s;
+        const float vn = sqrtf(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        if (nc < 0.0f && vn > 1e-30f) {
+          const float mag = fmaxf(0.0f, vn + nc * cl.friction);
+          const float inv = 1.0f / vn;
+#pragma unroll
+          for (int d = 0; d < 3; ++d) v[d] = v[d] * inv * mag;
+        }
+      }
+    }
+  } else {
+    const float r2 = off[0] * off[0] + off[1] * off[1] + off[2] * off[2];
+    if (r2 < cl.radius * cl.radius) {
+      if (cl.surface == 0) {
+        v[0] = v[1] = v[2] = 0.0f;
+      } else {
+        const float inv = 1.0f / (sqrtf(r2) + 1e-5f);
+        const float n3[3] = {off[0] * inv, off[1] * inv, off[2] * inv};
+        const float nc = n3[0] * v[0] + n3[1] * v[1] + n3[2] * v[2];
+        const float s = cl.surface == 1 ? nc : fminf(nc, 0.0f);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) v[d] = v[d] - n3[d] * s;
+      }
+    }
+  }
+}
+
+// Grid node update, engine/mpm_solver.py:586-598 (momentum to velocity and
+// gravity) followed by the post-process list in order.
 __device__ __forceinline__ float3 grid_node_update(const MpmParams &P, const int (&I)[3], float m,
                                                    float3 mv, float dt) {
   float v[3] = {mv.x, mv.y, mv.z};
@@ -351,57 +417,7 @@ __device__ __forceinline__ float3 grid_node_update(const MpmParams &P, const int
 #pragma unroll
     for (int d = 0; d < 3; ++d) v[d] = inv * v[d] + dt * P.gravity[d];
   }
-  for (int c = 0; c < P.n_colliders; ++c) {
-    const MpmCollider &cl = P.colliders[c];
-    if (cl.kind == 2) {  // bounding box, :600-616
-      const bool unb = cl.surface != 0;
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        const int lo = unb ? -P.grid_size / 2 + P.padding : P.padding;
-        const int hi = unb ? P.grid_size / 2 - P.padding : P.res[d] - P.padding;
-        if (I[d] < lo && v[d] < 0.0f) v[d] = 0.0f;
-        if (I[d] >= hi && v[d] > 0.0f) v[d] = 0.0f;
-      }
-      continue;
-    }
-    float off[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) off[d] = (float)I[d] * P.dx - cl.point[d];
-    if (cl.kind == 0) {
-      const float dn = off[0] * cl.normal[0] + off[1] * cl.normal[1] + off[2] * cl.normal[2];
-      if (dn < 0.0f) {
-        if (cl.surface == 0) {
-          v[0] = v[1] = v[2] = 0.0f;
-        } else {
-          const float nc = cl.normal[0] * v[0] + cl.normal[1] * v[1] + cl.normal[2] * v[2];
-          const float s = cl.surface == 1 ? nc : fminf(nc, 0.0f);
-#pragma unroll
-          for (int d = 0; d < 3; ++d) v[d] = v[d] - cl.normal[d] * s;
-          const float vn = sqrtf(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
-          if (nc < 0.0f && vn > 1e-30f) {
-            const float mag = fmaxf(0.0f, vn + nc * cl.friction);
-            const float inv = 1.0f / vn;
-#pragma unroll
-            for (int d = 0; d < 3; ++d) v[d] = v[d] * inv * mag;
-          }
-        }
-      }
-    } else {
-      const float r2 = off[0] * off[0] + off[1] * off[1] + off[2] * off[2];
-      if (r2 < cl.radius * cl.radius) {
-        if (cl.surface == 0) {
-          v[0] = v[1] = v[2] = 0.0f;
-        } else {
-          const float inv = 1.0f / (sqrtf(r2) + 1e-5f);
-          const float n3[3] = {off[0] * inv, off[1] * inv, off[2] * inv};
-          const float nc = n3[0] * v[0] + n3[1] * v[1] + n3[2] * v[2];
-          const float s = cl.surface == 1 ? nc : fminf(nc, 0.0f);
-#pragma unroll
-          for (int d = 0; d < 3; ++d) v[d] = v[d] - n3[d] * s;
-        }
-      }
-    }
-  }
+  for (int c = 0; c < P.n_colliders; ++c) postprocess_op(P, P.colliders[c], I, v);
   return make_float3(v[0], v[1], v[2]);
 }
 

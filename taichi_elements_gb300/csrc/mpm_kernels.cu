@@ -34,9 +34,6 @@ namespace mpm {
 constexpr int kP2GThreads = 128;
 constexpr int kG2PThreads = 128;
 
-__device__ __forceinline__ void set_status(const Ws &w, uint32_t bits) {
-  if (bits) atomicOr((unsigned int *)&w.counters[3], bits);
-}
 
 // ------------------------------------------------------------ binning ----
 
@@ -107,11 +104,6 @@ __global__ void k_bin_count(const MpmParams P, const MpmParams *tab, const Ws w,
   set_status(w, bad);
 }
 
-__device__ __forceinline__ void block_coords(const MpmParams &P, int64_t b, int &bx, int &by, int &bz) {
-  bz = (int)(b % P.win_nb[2]);
-  by = (int)((b / P.win_nb[2]) % P.win_nb[1]);
-  bx = (int)(b / ((int64_t)P.win_nb[1] * P.win_nb[2]));
-}
 
 // grid-active = some particle block b - d whose stencils reach b (bit d)
 __device__ __forceinline__ bool grid_flag(const MpmParams &P, const Ws &w, int64_t b) {

@@ -1,0 +1,105 @@
+"""Gradients of a final-state loss through a GPU rollout (float32 forward,
+hand-written adjoint, checkpointed segments) against two float64
+references: PyTorch autograd through oracle/torch_ref.py, and central
+finite differences of the C oracle along random directions.
+
+Tolerance: relative L2 error of dL/dv0 and dL/dE against the float64
+autograd gradient <= 3e-2, and each directional derivative within 3e-2 of
+the finite difference (relative to the gradient's norm times the direction's
+norm); float32 round-off over the rollout sets this bound.
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as O
+from oracle.torch_ref import TorchMPM, com_loss
+from taichi_elements_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+NSUB = 48
+K = 16
+
+
+def make_case(seed=3):
+    sc = scenes.elastic_on_water(res=32, n_each=1200)
+    rng = np.random.default_rng(seed)
+    n = sc.n
+    v0 = (sc.v + rng.normal(0.0, 0.3, (n, 3))).astype(np.float32)
+    E = np.exp(rng.uniform(np.log(2e4), np.log(2e5), n)).astype(np.float32)
+    return sc, v0, E
+
+
+def gpu_grads(sc, v0, E):
+    from taichi_elements_gb300.differentiable import Rollout, rollout_positions
+    from taichi_elements_gb300.mpm_solver import MPMSolver
+    s = MPMSolver(sc.res, per_particle_E=True)
+    for m in (0, 1):
+        sel = sc.material == m
+        s.add_particles(sc.x[sel], m, E=torch.as_tensor(E[sel]))
+    # particle ids follow the add order: water first, then elastic
+    order = np.concatenate([np.nonzero(sc.material == m)[0] for m in (0, 1)])
+    R = Rollout(s, NSUB, checkpoint_every=K)
+    v = torch.tensor(v0[order], device="cuda", requires_grad=True)
+    e = torch.tensor(E[order], device="cuda", requires_grad=True)
+    x = rollout_positions(R, v, e)
+    mat = torch.as_tensor(sc.material[order], device="cuda")
+    L = com_loss(x, mat, torch.tensor(sc.target, dtype=torch.float32, device="cuda"))
+    L.backward()
+    inv = np.argsort(order)
+    return (float(L), x.detach().cpu().numpy()[inv], v.grad.cpu().numpy()[inv], e.grad.cpu().numpy()[inv])
+
+
+def torch_grads(sc, v0, E):
+    T = TorchMPM(sc.res)
+    x0 = torch.tensor(sc.x, dtype=torch.float64)
+    v = torch.tensor(v0, dtype=torch.float64, requires_grad=True)
+    e = torch.tensor(E, dtype=torch.float64, requires_grad=True)
+    mat = torch.tensor(sc.material)
+    xT = T.rollout(x0, v, mat, e, sc.default_dt, NSUB)
+    L = com_loss(xT, mat, torch.tensor(sc.target))
+    L.backward()
+    return float(L), xT.detach().numpy(), v.grad.numpy(), e.grad.numpy()
+
+
+def test_adjoint_matches_float64_autograd():
+    sc, v0, E = make_case()
+    Lg, xg, gv, gE = gpu_grads(sc, v0, E)
+    Lr, xr, gv_r, gE_r = torch_grads(sc, v0, E)
+    assert np.abs(xg - xr).max() < 1e-4
+    assert abs(Lg - Lr) <= 1e-3 * abs(Lr) + 1e-9
+    ev = np.linalg.norm(gv - gv_r) / np.linalg.norm(gv_r)
+    eE = np.linalg.norm(gE - gE_r) / np.linalg.norm(gE_r)
+    assert ev < 3e-2, ev
+    assert eE < 3e-2, eE
+
+
+def test_adjoint_directional_derivatives_match_finite_differences():
+    sc, v0, E = make_case(seed=4)
+    _, _, gv, gE = gpu_grads(sc, v0, E)
+    cfg = O.Config(res=sc.res)
+    sel = sc.material == 1
+
+    def loss(v, e):
+        P = O.Particles.seeded(sc.x, sc.material, v=v.astype(np.float64), E=e.astype(np.float64))
+        R = O.Runner(cfg, P)
+        R.run(sc.default_dt, NSUB)
+        return float(((R.P.x[sel].mean(0) - sc.target)**2).sum())
+
+    rng = np.random.default_rng(7)
+    v0d, Ed = v0.astype(np.float64), E.astype(np.float64)
+
+    def close(gd, fd, g, d):
+        scale = np.linalg.norm(g) * np.linalg.norm(d) / np.sqrt(d.size)  # typical |<g, d>|
+        return abs(gd - fd) <= 3e-2 * max(abs(fd), scale)
+
+    for _ in range(3):
+        d = rng.standard_normal(v0.shape)
+        h = 1e-4
+        fd = (loss(v0d + h * d, Ed) - loss(v0d - h * d, Ed)) / (2 * h)
+        assert close((gv * d).sum(), fd, gv, d), ((gv * d).sum(), fd)
+        dE = rng.standard_normal(E.shape) * Ed
+        hE = 1e-4
+        fdE = (loss(v0d, Ed + hE * dE) - loss(v0d, Ed - hE * dE)) / (2 * hE)
+        assert close((gE * dE).sum(), fdE, gE * Ed, dE / Ed), ((gE * dE).sum(), fdE)

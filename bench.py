@@ -403,13 +403,17 @@ def run_adjoint_measure(n_substeps=2000, checkpoint_every=50):
     e = torch.tensor(np.concatenate([E[sc.material == m] for m in (0, 1)]), device="cuda")
     mat = torch.tensor(np.concatenate([sc.material[sc.material == m] for m in (0, 1)]), device="cuda")
     target = torch.tensor(sc.target, dtype=torch.float32, device="cuda")
-    init = R.initial_state(v0, e)
-    R._run(init, 20)  # warm-up
+    for _ in range(2):  # warm-up: first runs, then CUDA-graph capture
+        R.forward(v0, e, keep_checkpoints=False)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    R._run(init, n_substeps)
+    R.forward(v0, e, keep_checkpoints=False)  # plain forward rollout
     torch.cuda.synchronize()
     t_fwd = time.perf_counter() - t0
+    for _ in range(2):
+        v = v0.clone().requires_grad_(True)
+        ee = e.clone().requires_grad_(True)
+        com_loss(rollout_positions(R, v, ee), mat, target).backward()
     v = v0.clone().requires_grad_(True)
     ee = e.clone().requires_grad_(True)
     torch.cuda.synchronize()

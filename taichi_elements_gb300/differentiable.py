@@ -31,41 +31,53 @@ GROWS = 25  # dL/dx 3, dL/dv 3, dL/dC 9, dL/dF 9, dL/dJp 1
 class Rollout:
     """A fixed-length rollout of an MPMSolver's particles, differentiable in
     the initial velocities v0 (n,3) and per-particle E (n,), both indexed by
-    original particle id."""
+    original particle id.
 
-    def __init__(self, solver: MPMSolver, n_substeps: int, dt: float | None = None, checkpoint_every: int = 50):
+    Buffers are allocated once (checkpoints, one segment of states, two
+    gradient buffers), so each segment's forward, recomputation and adjoint
+    run as CUDA graphs after their first use."""
+
+    def __init__(self, solver: MPMSolver, n_substeps: int, dt: float | None = None, checkpoint_every: int = 50,
+                 use_cuda_graph: bool = True):
         if not solver.per_particle_E:
             raise ValueError("the differentiable rollout needs MPMSolver(per_particle_E=True)")
         self.s = solver
         self.n_substeps = int(n_substeps)
         self.dt = float(dt if dt is not None else solver.default_dt)
-        self.K = max(1, int(checkpoint_every))
+        self.K = max(1, min(int(checkpoint_every), self.n_substeps))
         self.n = solver.n_particles
+        self.use_cuda_graph = use_cuda_graph
         mats = torch.unique(solver.full_state()['material'])
         if not bool(torch.all((mats == 0) | (mats == 1))):
             raise NotImplementedError("gradients are implemented for water and elastic particles only")
         solver._prepare(self.dt * self.n_substeps)
         self.dev = solver.device
         self.cap = solver._cap
-        # initial state template (solver's current order)
-        self.init = solver._state[solver._cur].clone()
+        self.init = solver._state[solver._cur].clone()  # template in the solver's current order
         self.ids = self.init.view(torch.int32)[ROW_ID, :self.n].long()
         p = solver.params
         nbytes = ctypes.c_size_t(0)
         _lib.check(solver._lib.mpm_workspace_bytes(ctypes.byref(p), self.cap, ctypes.byref(nbytes)), "ws bytes")
-        self.ws = torch.empty(int(nbytes.value), dtype=torch.uint8, device=self.dev)
-        v = solver.views()
-        nodes = v['grid_mom'].shape[0]
+        self.ws = torch.zeros(int(nbytes.value), dtype=torch.uint8, device=self.dev)
+        nodes = solver.views()['grid_mom'].shape[0]
         self.keep = torch.zeros((nodes, 4), dtype=torch.float32, device=self.dev)
         self.ggrid = torch.zeros((nodes, 4), dtype=torch.float32, device=self.dev)
-        self.bufs = [torch.zeros_like(self.init) for _ in range(2)]
+        self.nseg = (self.n_substeps + self.K - 1) // self.K
+        self.a = torch.zeros_like(self.init)
+        self.b = torch.zeros_like(self.init)
+        self.ckpt = torch.zeros((self.nseg, NROWS, self.cap), dtype=torch.float32, device=self.dev)
+        self.ring = torch.zeros((self.K, NROWS, self.cap), dtype=torch.float32, device=self.dev)
         self.tmp = torch.zeros_like(self.init)
-        self.checkpoints = []
+        self.g = [torch.zeros((GROWS, self.cap), dtype=torch.float32, device=self.dev) for _ in range(2)]
+        self.gE = torch.zeros(self.cap, dtype=torch.float32, device=self.dev)
         sp = ctypes.c_void_p(0)
         _lib.check(solver._lib.mpm_status_ptr(ctypes.byref(p), self.ws.data_ptr(), self.cap, ctypes.byref(sp)),
                    "status")
         off = sp.value - self.ws.data_ptr()
         self.status = self.ws[off:off + 4].view(torch.int32)
+        self.status_acc = torch.zeros(1, dtype=torch.int32, device=self.dev)
+        self._graphs = {}
+        self._seen = set()
 
     # --------------------------------------------------------------- utils --
 
@@ -80,33 +92,88 @@ class Rollout:
     def _reset_ws(self):
         self._call("mpm_workspace_init", self.ws.data_ptr(), self.cap, self.stream)
 
+    def _bin(self, st):
+        self._call("mpm_bin_count", self.ws.data_ptr(), self.cap, st.data_ptr(), 0, self.n, self.stream)
+
+    def _collect_status(self):
+        torch.bitwise_or(self.status_acc, self.status, out=self.status_acc)
+
     def _check(self):
-        st = int(self.status.item())
+        st = int(self.status_acc.item())
         if st:
-            self.status.zero_()
+            self.status_acc.zero_()
             raise RuntimeError(f"MPM device status {st} in the differentiable rollout")
 
     def _substep(self, cur, nxt):
         self._call("mpm_substep", self.ws.data_ptr(), self.cap, self.n, cur.data_ptr(), nxt.data_ptr(), self.dt, None,
                    self.stream)
 
-    def _run(self, start_state, count, keep_every=None, keep_all=None):
-        """Run `count` substeps from a copy of start_state (binning it fresh);
-        returns the final buffer.  keep_every: append a checkpoint copy every
-        K substeps (before the substep); keep_all: list receiving the state
-        before every substep."""
-        a, b = self.bufs
-        a.copy_(start_state)
-        self._reset_ws()
-        self._call("mpm_bin_count", self.ws.data_ptr(), self.cap, a.data_ptr(), 0, self.n, self.stream)
-        for t in range(count):
-            if keep_every is not None and t % keep_every == 0:
-                self.checkpoints.append(a.clone())
-            if keep_all is not None:
-                keep_all.append(a.clone())
+    def _graphed(self, kind, count, fn):
+        """Run fn(count); from its second use on, as a captured CUDA graph."""
+        key = (kind, count)
+        g = self._graphs.get(key)
+        if g is None and self.use_cuda_graph and key in self._seen:
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                fn(count)
+            self._graphs[key] = g
+        if g is not None:
+            g.replay()
+        else:
+            self._seen.add(key)
+            fn(count)
+
+    def _seg_len(self, seg):
+        return min(self.K, self.n_substeps - seg * self.K)
+
+    # ----------------------------------------------------- segment bodies --
+
+    def _forward_ops(self, count):
+        """count substeps from self.a (already binned); result in self.a."""
+        a, b = self.a, self.b
+        for _ in range(count):
             self._substep(a, b)
             a, b = b, a
-        return a
+        if count % 2:
+            self.a.copy_(self.b)
+        self._collect_status()
+
+    def _recompute_ops(self, count):
+        """From self.a: ring[t] = state before substep t, t < count."""
+        self._reset_ws()
+        self._bin(self.a)
+        a, b = self.a, self.b
+        for t in range(count):
+            self.ring[t].copy_(a)
+            self._substep(a, b)
+            a, b = b, a
+        self._collect_status()
+        self._reset_ws()
+
+    def _adjoint_ops(self, count):
+        """Walk ring[count-1 .. 0] backwards; gradient stays in self.g[0]."""
+        gin, gout = self.g
+        for t in reversed(range(count)):
+            self._adjoint_substep(self.ring[t], gin, gout)
+            gin, gout = gout, gin
+        if count % 2:
+            self.g[0].copy_(self.g[1])
+        self._collect_status()
+
+    def _adjoint_substep(self, cur, gin, gout):
+        ws, cap, n, s = self.ws.data_ptr(), self.cap, self.n, self.stream
+        dt = self.dt
+        self._bin(cur)
+        self._call("mpm_bin_finalize", ws, cap, n, s)
+        self._call("mpm_p2g", ws, cap, n, cur.data_ptr(), self.tmp.data_ptr(), dt, s)
+        self._call("mpm_grid_snapshot", ws, cap, self.keep.data_ptr(), s)
+        self._call("mpm_grid_update", ws, cap, dt, s)
+        self.ggrid.zero_()
+        self._call("mpm_g2p_adj", ws, cap, n, self.tmp.data_ptr(), dt, gin.data_ptr(), gout.data_ptr(),
+                   self.ggrid.data_ptr(), s)
+        self._call("mpm_grid_adj", ws, cap, self.keep.data_ptr(), self.ggrid.data_ptr(), dt, s)
+        self._call("mpm_p2g_adj", ws, cap, n, cur.data_ptr(), self.tmp.data_ptr(), dt, gin.data_ptr(),
+                   gout.data_ptr(), self.ggrid.data_ptr(), self.gE.data_ptr(), s)
 
     # ------------------------------------------------------------- forward --
 
@@ -126,55 +193,40 @@ class Rollout:
         out[ids] = st[row0:row0 + ncols, :self.n].t()
         return out
 
-    def forward(self, v0: torch.Tensor, E: torch.Tensor) -> torch.Tensor:
-        """Final positions (n,3) by particle id; saves checkpoints."""
-        self.checkpoints = []
-        final = self._run(self.initial_state(v0, E), self.n_substeps, keep_every=self.K)
+    def _start(self, v0, E):
+        self.a.copy_(self.initial_state(v0, E))
+        self.status_acc.zero_()
+        self._reset_ws()
+        self._bin(self.a)
+
+    def forward(self, v0: torch.Tensor, E: torch.Tensor, keep_checkpoints: bool = True) -> torch.Tensor:
+        """Final positions (n,3) by particle id; saves the checkpoints."""
+        self._start(v0, E)
+        for seg in range(self.nseg):
+            if keep_checkpoints:
+                self.ckpt[seg].copy_(self.a)
+            self._graphed("fwd", self._seg_len(seg), self._forward_ops)
         torch.cuda.synchronize()
         self._check()
-        self.final = final.clone()
-        return self.by_id(final, ROW_X, 3)
+        return self.by_id(self.a, ROW_X, 3)
 
     # ------------------------------------------------------------ backward --
 
     def backward(self, gx_final: torch.Tensor):
         """dL/dv0 (n,3) and dL/dE (n,) by particle id, given dL/dx_final."""
-        n, cap = self.n, self.cap
-        gin = torch.zeros((GROWS, cap), dtype=torch.float32, device=self.dev)
-        gout = torch.zeros_like(gin)
-        gin[0:3, :n] = gx_final.to(self.dev, torch.float32).t()
-        gE = torch.zeros(cap, dtype=torch.float32, device=self.dev)
-        nseg = len(self.checkpoints)
-        for seg in reversed(range(nseg)):
-            t0 = seg * self.K
-            count = min(self.K, self.n_substeps - t0)
-            states = []
-            self._run(self.checkpoints[seg], count, keep_all=states)
-            self._reset_ws()
-            for t in reversed(range(count)):
-                cur = states[t]
-                self._adjoint_substep(cur, gin, gout, gE)
-                gin, gout = gout, gin
-            del states
+        n = self.n
+        for g in self.g:
+            g.zero_()
+        self.g[0][0:3, :n] = gx_final.to(self.dev, torch.float32).t()
+        self.gE.zero_()
+        for seg in reversed(range(self.nseg)):
+            count = self._seg_len(seg)
+            self.a.copy_(self.ckpt[seg])
+            self._graphed("rec", count, self._recompute_ops)
+            self._graphed("adj", count, self._adjoint_ops)
         torch.cuda.synchronize()
         self._check()
-        gv0 = gin[3:6, :n].t().contiguous()
-        return gv0, gE[:n].clone()
-
-    def _adjoint_substep(self, cur, gin, gout, gE):
-        ws, cap, n, s = self.ws.data_ptr(), self.cap, self.n, self.stream
-        dt = self.dt
-        self._call("mpm_bin_count", ws, cap, cur.data_ptr(), 0, n, s)
-        self._call("mpm_bin_finalize", ws, cap, n, s)
-        self._call("mpm_p2g", ws, cap, n, cur.data_ptr(), self.tmp.data_ptr(), dt, s)
-        self._call("mpm_grid_snapshot", ws, cap, self.keep.data_ptr(), s)
-        self._call("mpm_grid_update", ws, cap, dt, s)
-        self.ggrid.zero_()
-        self._call("mpm_g2p_adj", ws, cap, n, self.tmp.data_ptr(), dt, gin.data_ptr(), gout.data_ptr(),
-                   self.ggrid.data_ptr(), s)
-        self._call("mpm_grid_adj", ws, cap, self.keep.data_ptr(), self.ggrid.data_ptr(), dt, s)
-        self._call("mpm_p2g_adj", ws, cap, n, cur.data_ptr(), self.tmp.data_ptr(), dt, gin.data_ptr(),
-                   gout.data_ptr(), self.ggrid.data_ptr(), gE.data_ptr(), s)
+        return self.g[0][3:6, :n].t().contiguous(), self.gE[:n].clone()
 
 
 class _RolloutFunction(torch.autograd.Function):

@@ -164,7 +164,8 @@ __global__ __launch_bounds__(kAdjThreads) void k_g2p_adj(const MpmParams P, cons
       bool active = j < end;
       int cell = -1 - lane;
       int lx = 0, ly = 0, lz = 0;
-      float wt[3][3], fx[3] = {0.f, 0.f, 0.f}, Gvt[3] = {0.f, 0.f, 0.f}, GC[3][3];
+      float wt[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+      float fx[3] = {0.f, 0.f, 0.f}, Gvt[3] = {0.f, 0.f, 0.f}, GC[3][3];
 #pragma unroll
       for (int a = 0; a < 9; ++a) GC[a / 3][a % 3] = 0.0f;
       if (active) {
@@ -195,6 +196,7 @@ __global__ __launch_bounds__(kAdjThreads) void k_g2p_adj(const MpmParams P, cons
           if ((unsigned)lx > 3u || (unsigned)ly > 3u || (unsigned)lz > 3u) {
             bad |= MPM_STATUS_TABLE_OVERFLOW;
             active = false;
+            lx = ly = lz = 0;
           } else {
             cell = local_cell(lx, ly, lz);
             // dL/dfx through the weights and through (off - fx)
@@ -240,16 +242,15 @@ __global__ __launch_bounds__(kAdjThreads) void k_g2p_adj(const MpmParams P, cons
           for (int bb = 0; bb < 3; ++bb)
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-              if (mine) {
-                const float d[3] = {(float)a - fx[0], (float)bb - fx[1], (float)c - fx[2]};
-                const float wgt = wt[a][0] * wt[bb][1] * wt[c][2];
-                float4 *nd = tile + base_node + (a * kTileW + bb) * kTileW + c;
-                float4 g = *nd;
-                g.x += wgt * (Gvt[0] + s4 * (GC[0][0] * d[0] + GC[0][1] * d[1] + GC[0][2] * d[2]));
-                g.y += wgt * (Gvt[1] + s4 * (GC[1][0] * d[0] + GC[1][1] * d[1] + GC[1][2] * d[2]));
-                g.z += wgt * (Gvt[2] + s4 * (GC[2][0] * d[0] + GC[2][1] * d[1] + GC[2][2] * d[2]));
-                *nd = g;
-              }
+              // unconditional read and arithmetic, predicated store only
+              const float d[3] = {(float)a - fx[0], (float)bb - fx[1], (float)c - fx[2]};
+              const float wgt = wt[a][0] * wt[bb][1] * wt[c][2];
+              float4 *nd = tile + base_node + (a * kTileW + bb) * kTileW + c;
+              float4 g = *nd;
+              g.x += wgt * (Gvt[0] + s4 * (GC[0][0] * d[0] + GC[0][1] * d[1] + GC[0][2] * d[2]));
+              g.y += wgt * (Gvt[1] + s4 * (GC[1][0] * d[0] + GC[1][1] * d[1] + GC[1][2] * d[2]));
+              g.z += wgt * (Gvt[2] + s4 * (GC[2][0] * d[0] + GC[2][1] * d[1] + GC[2][2] * d[2]));
+              if (mine) *nd = g;
               __syncwarp();
             }
         if (!__any_sync(0xffffffffu, active && round_of_lane > round)) break;

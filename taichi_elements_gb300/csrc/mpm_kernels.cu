@@ -32,6 +32,10 @@
 namespace mpm {
 
 constexpr int kP2GThreads = 128;
+// P2G CTAs per SM the register budget is sized for (128 threads each)
+#ifndef MPM_P2G_MIN_CTAS
+#define MPM_P2G_MIN_CTAS 4
+#endif
 constexpr int kG2PThreads = 128;
 
 
@@ -363,12 +367,14 @@ __device__ __forceinline__ float4 f4add(float4 a, float4 b) {
 }
 
 template <bool HAS_EP, bool BATCH>
-__global__ __launch_bounds__(kP2GThreads, 5) void k_p2g(const MpmParams P, const MpmParams *tab, const Ws w,
+__global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_p2g(const MpmParams P, const MpmParams *tab, const Ws w,
                                                        const float *__restrict__ cur,
                                                        float *__restrict__ nxt, int64_t cap, float dt) {
-  __shared__ float4 tiles[kP2GWarps][kTileN];
+  // two tiles per warp: a lane whose cell already appears in an earlier lane
+  // of the same group (the second particle of a cell when a group straddles
+  // two short levels) scatters into the second tile in the same pass
+  __shared__ float4 tiles[kP2GWarps][2][kTileN];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float4 *tile = tiles[warp];
   const int nitems = (int)min((int64_t)w.counters[2], w.items_cap);
   uint32_t bad = 0;
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
@@ -377,7 +383,7 @@ __global__ __launch_bounds__(kP2GThreads, 5) void k_p2g(const MpmParams P, const
     const int end = (int)min((int64_t)min(start + P.chunk, w.pb_start[k] + w.pb_count[k]), cap);
     int bx, by, bz;
     block_coords(P, w.pblocks[k], bx, by, bz);
-    for (int t = lane; t < kTileN; t += 32) tile[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int t = lane; t < 2 * kTileN; t += 32) (&tiles[warp][0][0])[t] = make_float4(0.f, 0.f, 0.f, 0.f);
     __syncwarp();
     for (int j0 = start + warp * 32; j0 < end; j0 += kP2GThreads) {
       const int j = j0 + lane;
@@ -388,8 +394,9 @@ __global__ __launch_bounds__(kP2GThreads, 5) void k_p2g(const MpmParams P, const
         active = false;
       }
       int cell = -1 - lane;  // unique per inactive lane
-      float mass = 0.f, q[3] = {0.f, 0.f, 0.f}, adx[3][3];
-      float wt[3][3];
+      // inactive lanes keep zero weights: they read tile nodes but never store
+      float mass = 0.f, q[3] = {0.f, 0.f, 0.f}, adx[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+      float wt[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
       int lx = 0, ly = 0, lz = 0;
       if (active) {
         const float *src = cur + i;
@@ -432,6 +439,7 @@ __global__ __launch_bounds__(kP2GThreads, 5) void k_p2g(const MpmParams P, const
         if ((unsigned)lx > 3u || (unsigned)ly > 3u || (unsigned)lz > 3u) {  // moved since binning
           bad |= MPM_STATUS_TABLE_OVERFLOW;
           active = false;
+          lx = ly = lz = 0;
         } else {
           cell = local_cell(lx, ly, lz);
           bspline_weights(b.fx, wt);
@@ -447,11 +455,13 @@ __global__ __launch_bounds__(kP2GThreads, 5) void k_p2g(const MpmParams P, const
             for (int c = 0; c < 3; ++c) adx[r][c] = o.affine[r][c] * S.dx;
         }
       }
-      // lanes sharing a cell scatter in successive rounds
+      // The k-th lane (k = 0, 1, ...) of a group sharing a cell scatters into
+      // tile k % 2 in pass k / 2; inside one pass and tile all cells differ.
       const unsigned peers = __match_any_sync(0xffffffffu, cell);
       const int round_of_lane = __popc(peers & ((1u << lane) - 1u));
+      float4 *tile = tiles[warp][round_of_lane & 1];
       for (int round = 0;; ++round) {
-        const bool mine = active && round_of_lane == round;
+        const bool mine = active && (round_of_lane >> 1) == round;
         const int base_node = (lx * kTileW + ly) * kTileW + lz;
 #pragma unroll
         for (int a = 0; a < 3; ++a)
@@ -463,27 +473,27 @@ __global__ __launch_bounds__(kP2GThreads, 5) void k_p2g(const MpmParams P, const
             for (int d = 0; d < 3; ++d) pab[d] = q[d] + adx[d][0] * (float)a + adx[d][1] * (float)bb;
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-              if (mine) {
-                const float wgt = wab * wt[c][2];
-                float4 *nd = tile + base_node + (a * kTileW + bb) * kTileW + c;
-                float4 g = *nd;
-                g.x = fmaf(wgt, mass, g.x);
-                g.y = fmaf(wgt, pab[0] + adx[0][2] * (float)c, g.y);
-                g.z = fmaf(wgt, pab[1] + adx[1][2] * (float)c, g.z);
-                g.w = fmaf(wgt, pab[2] + adx[2][2] * (float)c, g.w);
-                *nd = g;
-              }
+              // unconditional read and arithmetic, predicated store only
+              const float wgt = wab * wt[c][2];
+              float4 *nd = tile + base_node + (a * kTileW + bb) * kTileW + c;
+              float4 g = *nd;
+              g.x = fmaf(wgt, mass, g.x);
+              g.y = fmaf(wgt, fmaf(adx[0][2], (float)c, pab[0]), g.y);
+              g.z = fmaf(wgt, fmaf(adx[1][2], (float)c, pab[1]), g.z);
+              g.w = fmaf(wgt, fmaf(adx[2][2], (float)c, pab[2]), g.w);
+              if (mine) *nd = g;
               __syncwarp();
             }
           }
-        if (!__any_sync(0xffffffffu, active && round_of_lane > round)) break;
+        if (!__any_sync(0xffffffffu, active && (round_of_lane >> 1) > round)) break;
       }
     }
     __syncthreads();
     for (int t = threadIdx.x; t < kTileN; t += blockDim.x) {
-      float4 g = tiles[0][t];
+      float4 g = tiles[0][0][t];
+      g = f4add(g, tiles[0][1][t]);
 #pragma unroll
-      for (int q = 1; q < kP2GWarps; ++q) g = f4add(g, tiles[q][t]);
+      for (int q = 1; q < kP2GWarps; ++q) g = f4add(f4add(g, tiles[q][0][t]), tiles[q][1][t]);
       if (g.x != 0.0f) {
         const int tx = t / 36, ty = (t / 6) % 6, tz = t % 6;
         const int gx = bx * 4 + tx, gy = by * 4 + ty, gz = bz * 4 + tz;

@@ -25,39 +25,39 @@ __device__ __forceinline__ float rsqrt_nr(float x) {
   return y * fmaf(-0.5f * x * y, y, 1.5f);
 }
 
+// 1/x to about 1 ulp: the hardware estimate refined by one Newton-Raphson
+// step for f(r) = 1/r - x, r <- r (2 - x r).
+__device__ __forceinline__ float rcp_nr(float x) {
+  const float r = __fdividef(1.0f, x);
+  return r * fmaf(-x, r, 2.0f);
+}
+
+// One Jacobi rotation in the (P, Q) plane, branch free.  With d = S_qq - S_pp
+// and a = S_pq, Rutishauser's t = sign(theta) / (|theta| + sqrt(theta^2 + 1)),
+// theta = d / (2a), is rewritten as t = 2 a sgn(d) / (|d| + sqrt(d^2 + 4a^2)),
+// which needs no division by a and gives t = 0 (no rotation) when a = 0.
 template <int P, int Q>
 __device__ __forceinline__ void jacobi_pair(float (&S)[3][3], float (&V)[3][3]) {
   constexpr int R = 3 - P - Q;
   const float apq = S[P][Q];
-  if (apq != 0.0f) {
-    // Rotation angle (Rutishauser): t = tan(angle).  Approximate division and
-    // square root suffice here: c and s below are renormalised, so U and V
-    // stay orthogonal, and the next sweep removes the residual off-diagonal.
-    const float theta = __fdividef(S[Q][Q] - S[P][P], 2.0f * apq);
-    const float at = fabsf(theta);
-    float t;
-    if (at > 1e15f) {
-      t = __fdividef(0.5f, theta);
-    } else {
-      const float r = fmaf(theta, theta, 1.0f);
-      t = __fdividef(1.0f, at + r * rsqrtf(r));
-      t = theta < 0.0f ? -t : t;
-    }
-    const float c = rsqrt_nr(fmaf(t, t, 1.0f));
-    const float s = t * c;
-    S[P][P] -= t * apq;
-    S[Q][Q] += t * apq;
-    S[P][Q] = 0.0f;
-    S[Q][P] = 0.0f;
-    const float srp = S[R][P], srq = S[R][Q];
-    S[R][P] = S[P][R] = c * srp - s * srq;
-    S[R][Q] = S[Q][R] = s * srp + c * srq;
+  const float d = S[Q][Q] - S[P][P];
+  const float r = fmaf(d, d, 4.0f * apq * apq);
+  const float den = fabsf(d) + r * rsqrtf(fmaxf(r, 1e-37f));
+  const float t = copysignf(2.0f, d) * apq * __fdividef(1.0f, fmaxf(den, 1e-37f));
+  const float c = rsqrt_nr(fmaf(t, t, 1.0f));
+  const float s = t * c;
+  S[P][P] -= t * apq;
+  S[Q][Q] += t * apq;
+  S[P][Q] = 0.0f;
+  S[Q][P] = 0.0f;
+  const float srp = S[R][P], srq = S[R][Q];
+  S[R][P] = S[P][R] = c * srp - s * srq;
+  S[R][Q] = S[Q][R] = s * srp + c * srq;
 #pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      const float vp = V[i][P], vq = V[i][Q];
-      V[i][P] = c * vp - s * vq;
-      V[i][Q] = s * vp + c * vq;
-    }
+  for (int i = 0; i < 3; ++i) {
+    const float vp = V[i][P], vq = V[i][Q];
+    V[i][P] = c * vp - s * vq;
+    V[i][Q] = s * vp + c * vq;
   }
 }
 
@@ -66,12 +66,10 @@ __device__ __forceinline__ void givens_qr_step(float (&B)[3][3], float (&U)[3][3
   // zero B[J][I] with a rotation of rows I and J; U accumulates G^T.
   const float a = B[I][I], b = B[J][I];
   const float r2 = fmaf(a, a, b * b);
-  float c = 1.0f, s = 0.0f;
-  if (r2 > 0.0f) {
-    const float ir = rsqrt_nr(r2);
-    c = a * ir;
-    s = b * ir;
-  }
+  const bool nz = r2 > 0.0f;
+  const float ir = rsqrt_nr(nz ? r2 : 1.0f);
+  const float c = nz ? a * ir : 1.0f;
+  const float s = nz ? b * ir : 0.0f;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     const float bi = B[I][k], bj = B[J][k];
@@ -129,14 +127,13 @@ __device__ __forceinline__ bool polar_rotation(const float (&F)[3][3], float (&R
     Cf[2][1] = R[0][2] * R[1][0] - R[0][0] * R[1][2];
     Cf[2][2] = R[0][0] * R[1][1] - R[0][1] * R[1][0];
     const float det = R[0][0] * Cf[0][0] + R[0][1] * Cf[0][1] + R[0][2] * Cf[0][2];
-    const float h = 0.5f / det;
-    change = 0.0f;
+    const float h = 0.5f * rcp_nr(det);
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
         const float r = fmaf(0.5f, R[i][j], h * Cf[i][j]);
-        change = fmaxf(change, fabsf(r - R[i][j]));
+        if (it == ITERS - 1) change = fmaxf(change, fabsf(r - R[i][j]));
         R[i][j] = r;
       }
   }

@@ -230,17 +230,39 @@ __device__ __forceinline__ P2GOut constitutive(const MpmParams &P, float dt, int
     Fn[0][0] = J;
     Jp = J;
   } else {
-    if (mat == 1 || mat == 4) {
-      // Elastic and stationary particles never clamp sigma (:527-536), so
-      // J = s0*s1*s2 = det(Fn) and the corotated stress needs only the
-      // rotation R = U V^T, which for det Fn > 0 is the polar factor.
-      // Inverted or extremely stretched Fn takes the SVD below, which keeps
-      // the reference's rotation-only convention for det Fn < 0.
+    if (mat == 1 || mat == 4 || mat == 2) {
+      // Elastic and stationary particles never clamp sigma (:527-536), and a
+      // snow particle whose singular values all lie inside the clamp range
+      // [1 - 2.5e-2, 1 + 4.5e-3] is not clamped either (Jp *= s/s = 1, F is
+      // reconstructed unchanged).  Then J = s0*s1*s2 = det(Fn) and the
+      // corotated stress needs only the rotation R = U V^T, which for
+      // det Fn > 0 is the polar factor.  The singular values are the
+      // eigenvalues of the symmetric stretch S = R^T Fn; the snow test checks
+      // that every Gershgorin disc of S lies inside the clamp range.
+      // Inverted, extremely stretched or clamped particles take the SVD below,
+      // which keeps the reference's rotation-only convention for det Fn < 0.
       const float J = Fn[0][0] * (Fn[1][1] * Fn[2][2] - Fn[1][2] * Fn[2][1]) -
                       Fn[0][1] * (Fn[1][0] * Fn[2][2] - Fn[1][2] * Fn[2][0]) +
                       Fn[0][2] * (Fn[1][0] * Fn[2][1] - Fn[1][1] * Fn[2][0]);
       float R[3][3];
-      if (J > 0.0f && polar_rotation<5>(Fn, R)) {
+      bool ok = J > 0.0f && polar_rotation<6>(Fn, R);
+      if (ok && mat == 2) {
+        float S[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) S[i][j] = R[0][i] * Fn[0][j] + R[1][i] * Fn[1][j] + R[2][i] * Fn[2][j];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          float rad = 0.0f;
+#pragma unroll
+          for (int j = 0; j < 3; ++j)
+            if (j != i) rad += 0.5f * (fabsf(S[i][j]) + fabsf(S[j][i]));
+          // margin of 4e-7 covers the float32 error of S
+          ok = ok && (S[i][i] - rad - 4e-7f >= 1.0f - 2.5e-2f) && (S[i][i] + rad + 4e-7f <= 1.0f + 4.5e-3f);
+        }
+      }
+      if (ok) {
         const float lj = la * J * (J - 1.0f);
 #pragma unroll
         for (int i = 0; i < 3; ++i)

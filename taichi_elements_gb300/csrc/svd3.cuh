@@ -104,18 +104,19 @@ __device__ __forceinline__ void cond_swap(bool doit, float (&B)[3][3], float (&V
 // Rotation factor R of the polar decomposition F = R S by Newton's
 // iteration R <- (R + R^{-T}) / 2 (Higham, "Computing the polar
 // decomposition - with applications", 1986), starting from R = F.  Valid for
-// det F > 0, where R equals U V^T of the SVD convention above.  Returns false
-// when the last step still moved R by more than `tol` (very large stretch), in
-// which case the caller uses the SVD.
-template <int ITERS = 5>
-__device__ __forceinline__ bool polar_rotation(const float (&F)[3][3], float (&R)[3][3], float tol = 2e-6f) {
+// det F > 0, where R equals U V^T of the SVD convention above.  Newton's
+// iteration converges quadratically: once a step moves R by at most 3e-4 the
+// remaining error is below about 5e-8, so the loop stops there.  Returns false
+// when that has not happened after MAX_ITERS steps (very large stretch); the
+// caller then uses the SVD.
+template <int MAX_ITERS = 6>
+__device__ __forceinline__ bool polar_rotation(const float (&F)[3][3], float (&R)[3][3]) {
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j) R[i][j] = F[i][j];
-  float change = 0.0f;
-#pragma unroll
-  for (int it = 0; it < ITERS; ++it) {
+  bool done = false;
+  for (int it = 0; it < MAX_ITERS && !done; ++it) {
     float Cf[3][3];  // cofactor matrix: R^{-T} = Cf / det
     Cf[0][0] = R[1][1] * R[2][2] - R[1][2] * R[2][1];
     Cf[0][1] = R[1][2] * R[2][0] - R[1][0] * R[2][2];
@@ -128,16 +129,18 @@ __device__ __forceinline__ bool polar_rotation(const float (&F)[3][3], float (&R
     Cf[2][2] = R[0][0] * R[1][1] - R[0][1] * R[1][0];
     const float det = R[0][0] * Cf[0][0] + R[0][1] * Cf[0][1] + R[0][2] * Cf[0][2];
     const float h = 0.5f * rcp_nr(det);
+    float change = 0.0f;
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
         const float r = fmaf(0.5f, R[i][j], h * Cf[i][j]);
-        if (it == ITERS - 1) change = fmaxf(change, fabsf(r - R[i][j]));
+        change = fmaxf(change, fabsf(r - R[i][j]));
         R[i][j] = r;
       }
+    done = change <= 3e-4f;
   }
-  return change <= tol;
+  return done;
 }
 
 template <int SWEEPS = 4>

@@ -153,6 +153,21 @@ def allmax(x, ws):
     return float(t.item())
 
 
+def p2g_traffic(n_particles):
+    """k_p2g DRAM bytes per launch: the per-particle figure of the committed
+    ncu capture (profiles/dram_four_materials_128.txt) times the particle
+    count, or None when the summary is absent."""
+    path = os.path.join(ROOT, "profiles", "dram_four_materials_128.txt")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for line in f:
+            parts = line.split()
+            if len(parts) == 2 and parts[0] == "k_p2g_dram_bytes_per_particle":
+                return float(parts[1]) * n_particles
+    return None
+
+
 def count_nodes(solver):
     """Distinct grid nodes touched by particle stencils (mass > 0)."""
     import torch
@@ -232,13 +247,7 @@ def run_gb300(args):
     sub_bytes = ALGO_BYTES_PER_PARTICLE * n + ALGO_BYTES_PER_NODE * n_nodes
     sub_ach = sub_bytes / ((ph_mean[1] + ph_mean[2] + ph_mean[3]) / 1e3) / 1e9
     full_ach = sub_bytes / (ph.sum(1).mean() / 1e3) / 1e9
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tp):
-        with open(tp) as f:
-            tj = json.load(f)
-        t = tj.get(args.workload, {}).get("p2g_dram_bytes_per_launch")
-        traffic = t
+    traffic = p2g_traffic(n)
 
     e2e = None
     if not args.no_e2e:

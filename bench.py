@@ -188,6 +188,11 @@ def run_gb300(args):
     sc = make_scene(args.workload)
     solver = sc.make_solver(chunk=args.chunk) if args.chunk else sc.make_solver()
     dt = sc.default_dt
+    chunk_times = None
+    if not args.chunk:
+        from taichi_elements_gb300.autotune import time_chunks, tune_chunk
+        chunk_times = time_chunks(solver)
+        tune_chunk(solver)
     lib = solver._lib
     stream = torch.cuda.current_stream()
     sptr = stream.cuda_stream
@@ -283,6 +288,7 @@ def run_gb300(args):
             "l2": f"inputs larger than L2: particle state {n * 212 / 1e9:.2f} GB per buffer pair",
             "parallelism": f"replicas x{ws}",
             "chunk": solver.chunk,
+            "chunk_ms_per_substep": chunk_times,
         },
         "phases_ms": {"binning": ph_mean[0], "p2g": ph_mean[1], "grid": ph_mean[2], "g2p": ph_mean[3]},
         "roofline": {"bound": "hbm", "kernel": "k_p2g", "achieved": p2g_ach, "peak": peak, "unit": "GB/s",
@@ -407,6 +413,8 @@ def run_adjoint_measure(n_substeps=2000, checkpoint_every=50):
     for m in (0, 1):
         sel = sc.material == m
         s.add_particles(sc.x[sel], m, E=torch.as_tensor(E[sel]))
+    from taichi_elements_gb300.autotune import tune_chunk
+    tune_chunk(s)
     R = Rollout(s, n_substeps, checkpoint_every=checkpoint_every)
     v0 = torch.zeros((sc.n, 3), device="cuda")
     e = torch.tensor(np.concatenate([E[sc.material == m] for m in (0, 1)]), device="cuda")
@@ -434,7 +442,7 @@ def run_adjoint_measure(n_substeps=2000, checkpoint_every=50):
     t_all = time.perf_counter() - t0
     return {"value": sc.n * n_substeps / t_all, "unit": "particle-substeps/s (forward+adjoint)",
             "plain_forward_value": sc.n * n_substeps / t_fwd, "fwd_adjoint_over_forward": t_all / t_fwd,
-            "particles": sc.n, "substeps": n_substeps, "checkpoint_every": checkpoint_every,
+            "particles": sc.n, "substeps": n_substeps, "checkpoint_every": checkpoint_every, "chunk": s.chunk,
             "seconds_forward": t_fwd, "seconds_forward_adjoint": t_all,
             "grad_norms": {"v0": float(v.grad.norm()), "E": float(ee.grad.norm())},
             "workload": "64^3 grid, elastic cube 100K on water slab 100K, per-particle E, f32, "
@@ -515,7 +523,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=None)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="ellipsoids_256",
-                    choices=["ellipsoids_256", "four_materials_128", "water_cube_64"])
+                    choices=["ellipsoids_256", "four_materials_128", "water_cube_64", "elastic_on_water"])
     ap.add_argument("--chunk", type=int, default=None)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -525,6 +533,9 @@ def main():
     ap.add_argument("--e2e-frames", type=int, default=3)
     ap.add_argument("--e2e-substeps", type=int, default=50)
     args = ap.parse_args()
+    if args.workload == "elastic_on_water":  # the differentiable workload alone
+        print(json.dumps(run_adjoint_measure(n_substeps=args.steps or 2000)))
+        return
     if args.impl == "reference":
         args.steps = 3 if args.steps is None else args.steps
         args.warmup = 1 if args.warmup is None else args.warmup

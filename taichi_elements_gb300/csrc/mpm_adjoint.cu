@@ -407,8 +407,11 @@ __global__ __launch_bounds__(kAdjThreads) void k_p2g_adj(const MpmParams P, cons
       const float J = Fn[0][0] * Cf[0][0] + Fn[0][1] * Cf[0][1] + Fn[0][2] * Cf[0][2];
       const float h = mat == 1 ? 0.3f : 1.0f;
       const float mu = mat == 0 ? 0.0f : mu0 * h, la = la0 * h;
+      // Rotation R = U V^T of Fn: the Newton polar factor when det Fn > 0 (as
+      // in the forward), else from the SVD (inverted / extreme stretch).
       float U[3][3], sg[3], V[3][3], R[3][3];
-      if (mat == 1) {
+      const bool polar_ok = mat == 1 && J > 0.0f && polar_rotation<6>(Fn, R);
+      if (mat == 1 && !polar_ok) {
         svd3<4>(Fn, U, sg, V);
 #pragma unroll
         for (int r = 0; r < 3; ++r)
@@ -508,6 +511,41 @@ __global__ __launch_bounds__(kAdjThreads) void k_p2g_adj(const MpmParams P, cons
             gR[r][c] = -gD;
             gmu += gS[r][c] * 2.0f * (D[r][0] * Fn[c][0] + D[r][1] * Fn[c][1] + D[r][2] * Fn[c][2]);
           }
+        if (polar_ok) {
+          // Polar backward without an SVD: with S = R^T Fn and dR = R [w]x,
+          // S[w]x + [w]x S = [(tr S I - S) w]x gives
+          // dL/dFn += R [z]x, z = (tr S I - S)^{-1} axial(R^T gR),
+          // axial(X) = (X21 - X12, X02 - X20, X10 - X01); the eigenvalues of
+          // tr S I - S are the sums s_i + s_j, kept away from zero.
+          float S[3][3], M[3][3];
+#pragma unroll
+          for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              S[r][c] = R[0][r] * Fn[0][c] + R[1][r] * Fn[1][c] + R[2][r] * Fn[2][c];
+              M[r][c] = R[0][r] * gR[0][c] + R[1][r] * gR[1][c] + R[2][r] * gR[2][c];
+            }
+          const float trS = S[0][0] + S[1][1] + S[2][2];
+          float A[3][3];
+#pragma unroll
+          for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) A[r][c] = (r == c ? trS : 0.0f) - 0.5f * (S[r][c] + S[c][r]);
+          const float mv[3] = {M[2][1] - M[1][2], M[0][2] - M[2][0], M[1][0] - M[0][1]};
+          float Ac[3][3];
+          cofactor(A, Ac);
+          float detA = A[0][0] * Ac[0][0] + A[0][1] * Ac[0][1] + A[0][2] * Ac[0][2];
+          if (fabsf(detA) < 1e-12f) detA = detA < 0.0f ? -1e-12f : 1e-12f;
+          const float id = 1.0f / detA;
+          float z[3];
+#pragma unroll
+          for (int r = 0; r < 3; ++r) z[r] = id * (Ac[0][r] * mv[0] + Ac[1][r] * mv[1] + Ac[2][r] * mv[2]);
+          const float Zx[3][3] = {{0.0f, -z[2], z[1]}, {z[2], 0.0f, -z[0]}, {-z[1], z[0], 0.0f}};
+#pragma unroll
+          for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) gFn[r][c] += R[r][0] * Zx[0][c] + R[r][1] * Zx[1][c] + R[r][2] * Zx[2][c];
+        } else {
         // polar rotation R = U V^T: dF = U [K o (M - M^T)] V^T with
         // M = U^T gR V and K_ij = 1 / (s_i + s_j), clamped away from zero
         float M[3][3];
@@ -542,6 +580,7 @@ __global__ __launch_bounds__(kAdjThreads) void k_p2g_adj(const MpmParams P, cons
               for (int q = 0; q < 3; ++q) acc += U[r][p] * Kx[p][q] * V[c][q];
             gFn[r][c] += acc;
           }
+        }
         if (perE) gEv = h * (dmu0 * gmu + dla0 * J * (J - 1.0f) * trgS);
         gJp_out = GJpo;
       }

@@ -14,7 +14,7 @@ namespace mpm {
 constexpr int kBlockCells = 64;  // 4^3 leaf block (engine/mpm_solver.py:159)
 constexpr int kTileW = 6;        // block + 2-node halo along each axis
 constexpr int kTileN = kTileW * kTileW * kTileW;
-constexpr int kFlagTile = 2048;  // window blocks per flag-compaction CTA
+constexpr int kFlagTile = 512;   // window blocks per flag-compaction CTA
 constexpr int kStatTile = 256;   // particle blocks per stats CTA
 
 // Row indices of the particle state buffer (see include/mpm_gb300.h).

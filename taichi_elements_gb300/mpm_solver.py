@@ -16,8 +16,8 @@ machine without a CUDA device, or without the built library, raises.
 Extensions beyond the reference: ``substep(dt)``, per-particle Young's
 modulus (``per_particle_E=True`` and the ``E`` argument of the seeding
 calls), ``state_dict``/``load_state_dict`` (exact checkpoints of x, v, C, F,
-Jp), ``tensors()`` (zero-copy device views) and CUDA-graph capture of whole
-frames.
+Jp), ``tensors()`` (zero-copy device views), CUDA-graph capture of whole
+frames and a measured choice of the work-item size (``autotune=True``).
 """
 from __future__ import annotations
 
@@ -91,7 +91,8 @@ class MPMSolver:
                  seed=0,
                  chunk=None,
                  use_cuda_graph=True,
-                 per_particle_E=False):
+                 per_particle_E=False,
+                 autotune=False):
         self.dim = len(res)
         assert self.dim in (2, 3), "MPM solver supports only 2D and 3D simulations."
         if self.dim != 3:
@@ -156,6 +157,8 @@ class MPMSolver:
         self.per_particle_E = bool(per_particle_E)
         self.chunk = int(chunk) if chunk else self.DEFAULT_CHUNK
         self.use_cuda_graph = use_cuda_graph
+        self.autotune = bool(autotune)
+        self._tuned = False
         self.gravity = (0.0, -9.8, 0.0)
         self.grid_postprocess = []  # records: dicts with kind/surface/...
         self.add_bounding_box(self.unbounded)
@@ -602,6 +605,10 @@ class MPMSolver:
         if print_stat:
             print(f'needed substeps: {int(frame_dt / self.default_dt) + 1}')
         self._prepare(frame_dt)
+        if self.autotune and not self._tuned and self.n_particles > 0:
+            from .autotune import tune_chunk
+            tune_chunk(self)
+            self._tuned = True
         if self.n_particles > 0:
             self._run_frame(count, dt)
             maxv = self._maxv[:count].cpu().numpy()

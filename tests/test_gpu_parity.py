@@ -282,3 +282,17 @@ def test_golden_fixture_one_substep(name):
         eg = np.abs(st[f] - g["out_" + f]).max() / scale
         e32 = np.abs(getattr(P32, f) - g["out_" + f]).max() / scale
         assert eg <= max(1e-6, 4 * e32), f"{f}: gpu {eg:.3g} f32 oracle {e32:.3g}"
+
+
+def test_autotune_picks_a_candidate_and_leaves_state_untouched():
+    from taichi_elements_gb300.autotune import CANDIDATES, tune_chunk
+    sc = scenes.smoke_scene()
+    s = sc.make_solver()
+    before = s.full_state()['x'].clone()
+    c = tune_chunk(s)
+    assert c in CANDIDATES and s.chunk == c
+    assert torch.equal(s.full_state()['x'], before)
+    s.step(2e-3)
+    ref = sc.make_solver(chunk=512)
+    ref.step(2e-3)
+    assert np.abs(s.particle_info()['position'] - ref.particle_info()['position']).max() < 1e-5

@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define MPM_ABI_VERSION 2
+#define MPM_ABI_VERSION 3
 #define MPM_NROWS 28
 #define MPM_MAX_COLLIDERS 16 /* post-process records, box included */
 
@@ -167,27 +167,48 @@ int mpm_batch_substep(const MpmParams *p, const MpmParams *scenes, void *ws, int
 
 /* ---- Adjoint of one substep (water and elastic) ----------------------
  * No counterpart in the reference, which has no autodiff.  Gradient buffers
- * `gin` / `gout` have 25 float32 rows of `cap` elements indexed by ORIGINAL
- * particle id: dL/dx (rows 0-2), dL/dv (3-5), dL/dC (6-14), dL/dF (15-23),
- * dL/dJp (24); `gin` holds the gradient with respect to the state after
- * substep t, `gout` receives the one before it.  `gE` (float[cap], by id)
- * accumulates dL/dE for per-particle Young's modulus.  `keep` and `ggrid`
- * are float4 arrays shaped like the workspace grid (see mpm_workspace_bytes:
- * window blocks * 64 nodes).
- * Sequence for substep t, after re-running its forward (bin, finalize, p2g)
- * from the state before it (`cur`) into `st`:
+ * `gin` / `gout` have 26 float32 rows of `cap` columns: dL/dx (rows 0-2),
+ * dL/dv (3-5), dL/dC (6-14), dL/dF (15-23), dL/dJp (24) and dL/dE of the
+ * per-particle Young's modulus (25); `gin` holds the gradient with respect to
+ * the state after substep t, `gout` receives the one before it (distinct
+ * buffers).  Columns are original particle ids when `by_id` is nonzero;
+ * otherwise `gin` is in the order of the substep's sorted output (the order
+ * mpm_p2g wrote `nxt` in) and `gout` in the order of `cur`, so all gradient
+ * traffic is coalesced.  `gmid` (3 rows of `cap`) carries the position
+ * gradient from mpm_g2p_adj to mpm_p2g_adj.  `keep` and `ggrid` are float4
+ * arrays shaped like the workspace grid (see mpm_workspace_bytes: window
+ * blocks * 64 nodes).
+ * `cur` is the particle state before substep t.  The workspace `ws` must
+ * hold the binning and grid of the forward substep t: run its forward
+ * (bin count, finalize, p2g from `cur`), then
  *   mpm_grid_snapshot(keep)      - between mpm_p2g and mpm_grid_update
  *   mpm_grid_update
- *   zero ggrid; mpm_g2p_adj      - writes gout rows 0-2, scatters dL/dv_grid
+ * (a caller may do this during a checkpoint-segment recompute and keep one
+ * workspace + snapshot per substep), and then for the adjoint:
+ *   zero ggrid; mpm_g2p_adj      - writes gmid, scatters dL/dv_grid
  *   mpm_grid_adj                 - dL/dv_grid -> dL/d(m, mv) in place
- *   mpm_p2g_adj                  - adds to gout rows 0-2, writes rows 3-24 */
+ *   mpm_p2g_adj                  - writes all rows of gout */
 int mpm_grid_snapshot(const MpmParams *p, void *ws, int64_t cap, float *keep, void *stream);
-int mpm_g2p_adj(const MpmParams *p, void *ws, int64_t cap, int64_t n, const float *st, float dt, const float *gin,
-                float *gout, float *ggrid, void *stream);
+/* Move `rows` gradient rows (row stride cap) between original-id columns and
+ * the column order of particle state `state`: with to_state_order nonzero
+ * dst[r][j] = src[r][id_j], else dst[r][id_j] = src[r][j], where id_j is the
+ * id row of `state` at column j.  src and dst must differ. */
+int mpm_grad_reorder(const float *state, int64_t cap, int64_t n, int32_t rows, const float *src, float *dst,
+                     int32_t to_state_order, void *stream);
+/* mpm_g2p with the next substep's binning (cell counts, block flags, cell
+ * keys) written to the workspace `ws_bins` instead of `ws`, so that a
+ * checkpoint-segment recompute can keep one workspace per substep.  The cell
+ * counts and block flags of `ws_bins` must be zero: a freshly initialised
+ * workspace, or one whose own substep (bin finalize) has run since it was
+ * last binned into. */
+int mpm_g2p_bin_into(const MpmParams *p, void *ws, void *ws_bins, int64_t cap, int64_t n, float *nxt, float dt,
+                     float *maxv_out, void *stream);
+int mpm_g2p_adj(const MpmParams *p, void *ws, int64_t cap, int64_t n, const float *cur, float dt, const float *gin,
+                float *gmid, float *ggrid, int32_t by_id, void *stream);
 int mpm_grid_adj(const MpmParams *p, void *ws, int64_t cap, const float *keep, float *ggrid, float dt,
                  void *stream);
-int mpm_p2g_adj(const MpmParams *p, void *ws, int64_t cap, int64_t n, const float *cur, const float *st, float dt,
-                const float *gin, float *gout, const float *ggrid, float *gE, void *stream);
+int mpm_p2g_adj(const MpmParams *p, void *ws, int64_t cap, int64_t n, const float *cur, float dt, const float *gin,
+                const float *gmid, float *gout, const float *ggrid, int32_t by_id, void *stream);
 
 /* One substep that allocates nothing and needs no caller-provided workspace.
  * No counterpart in the reference: it exists for callers that cannot call

@@ -12,7 +12,7 @@ from pathlib import Path
 
 from . import build as _build
 
-ABI_VERSION = 2
+ABI_VERSION = 3
 NROWS = 28
 MAX_COLLIDERS = 16
 
@@ -106,9 +106,11 @@ SIGNATURES = {
     "mpm_substep_noalloc": [_P, _i64, _i64, _v, _v, _f, _v, _v],
     "mpm_batch_bin_count": [_P, _v, _v, _i64, _v, _i64, _i64, _v],
     "mpm_grid_snapshot": [_P, _v, _i64, _v, _v],
-    "mpm_g2p_adj": [_P, _v, _i64, _i64, _v, _f, _v, _v, _v, _v],
+    "mpm_g2p_bin_into": [_P, _v, _v, _i64, _i64, _v, _f, _v, _v],
+    "mpm_grad_reorder": [_v, _i64, _i64, _i32, _v, _v, _i32, _v],
+    "mpm_g2p_adj": [_P, _v, _i64, _i64, _v, _f, _v, _v, _v, _i32, _v],
     "mpm_grid_adj": [_P, _v, _i64, _v, _v, _f, _v],
-    "mpm_p2g_adj": [_P, _v, _i64, _i64, _v, _v, _f, _v, _v, _v, _v, _v],
+    "mpm_p2g_adj": [_P, _v, _i64, _i64, _v, _f, _v, _v, _v, _v, _i32, _v],
     "mpm_batch_substep": [_P, _v, _v, _i64, _i64, _v, _v, _v, _v],
     "mpm_gather_rows": [_v, _i64, _i64, _i32, _i32, _v, _v],
     "mpm_status_ptr": [_P, _v, _i64, ctypes.POINTER(ctypes.c_void_p)],

@@ -4,9 +4,10 @@
 // differentiates is the substep of engine/mpm_solver.py:487-724 as restated
 // by mpm_kernels.cu.
 //
-// Per substep t, in reverse order (the forward of substep t is re-run first
-// so that the sorted order, the grid momentum snapshot `keep` and the grid
-// velocity are those of substep t):
+// Per substep t, in reverse order, given the workspace of the forward
+// substep t (its binning and sorted order, the grid momentum snapshot `keep`
+// taken before the grid update, and the grid velocity) and the particle state
+// `cur` before the substep:
 //   k_g2p_adj   reverse of G2P (:694-724): particle gradients of x', v', C'
 //               give grid-velocity gradients (scattered through per-warp
 //               shared-memory tiles, like P2G) and the weight / position part
@@ -16,8 +17,10 @@
 //               then v = mv/m + dt g.
 //   k_p2g_adj   reverse of P2G (:487-584): grid gradients gathered at the
 //               particle, the constitutive update recomputed and reversed
-//               (stress, det, polar rotation through the SVD with clamped
-//               1/(s_i + s_j) terms, (I + dt C) F), giving dL/d(x, v, C, F,
+//               (stress, det, polar rotation R of F = R S through
+//               (tr(S) I - S)^-1 acting on axial(R^T dR), or through the
+//               SVD with clamped 1/(s_i + s_j) terms where S is not positive
+//               definite, (I + dt C) F), giving dL/d(x, v, C, F,
 //               Jp) of substep t and accumulating dL/dE per particle.
 // Gradient buffers are indexed by original particle id, so the sorted orders
 // of the forward and of the recomputation need not agree.
@@ -28,8 +31,9 @@
 
 namespace mpm {
 
-// rows of a gradient buffer (float32, row stride = cap, indexed by id)
-enum GRow : int { gX = 0, gV = 3, gC = 6, gF = 15, gJp = 24 };
+// rows of a gradient buffer (float32, row stride = cap): dL/d(x, v, C, F,
+// Jp, per-particle E) of one particle state
+enum GRow : int { gX = 0, gV = 3, gC = 6, gF = 15, gJp = 24, gE = 25 };
 
 constexpr int kAdjThreads = 128;
 constexpr int kAdjWarps = kAdjThreads / 32;
@@ -133,9 +137,15 @@ __global__ __launch_bounds__(256) void k_grid_snapshot(const MpmParams P, const 
 
 // ------------------------------------------------------------- G2P adj ----
 
-__global__ __launch_bounds__(kAdjThreads) void k_g2p_adj(const MpmParams P, const Ws w, const float *__restrict__ st,
+// Gradient indexing: with BY_ID, gradient columns are original particle ids;
+// otherwise `gin` is in the order of the sorted substep output (column j)
+// and `gout` in the order of the substep input `cur` (column pid[j]).  The
+// position part of dL/dx from G2P goes to `gmid` (3 rows, column j) and is
+// added into `gout` by k_p2g_adj.
+template <bool BY_ID>
+__global__ __launch_bounds__(kAdjThreads) void k_g2p_adj(const MpmParams P, const Ws w, const float *__restrict__ cur,
                                                          int64_t cap, float dt, const float *__restrict__ gin,
-                                                         float *__restrict__ gout, float4 *__restrict__ ggrid) {
+                                                         float *__restrict__ gmid, float4 *__restrict__ ggrid) {
   __shared__ float4 vt[kTileN];
   __shared__ float4 tiles[kAdjWarps][kTileN];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -168,25 +178,34 @@ __global__ __launch_bounds__(kAdjThreads) void k_g2p_adj(const MpmParams P, cons
       float fx[3] = {0.f, 0.f, 0.f}, Gvt[3] = {0.f, 0.f, 0.f}, GC[3][3];
 #pragma unroll
       for (int a = 0; a < 9; ++a) GC[a / 3][a % 3] = 0.0f;
+      const int64_t i = active ? (int64_t)w.pid[j] : 0;
+      if (active && (i < 0 || i >= cap)) {
+        bad |= MPM_STATUS_TABLE_OVERFLOW;
+        active = false;
+      }
+      const int64_t gi = !active ? 0 : BY_ID ? (int64_t)__float_as_int(cur[kId * cap + i]) : (int64_t)j;
+      if (active && (gi < 0 || gi >= cap)) {  // corrupted id row
+        bad |= MPM_STATUS_TABLE_OVERFLOW;
+        active = false;
+      }
       if (active) {
-        const int64_t id = __float_as_int(st[kId * cap + j]);
-        const int mat = __float_as_int(st[kMat * cap + j]) & 0xFF;
+        const int mat = __float_as_int(cur[kMat * cap + i]) & 0xFF;
         float Gx[3];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) Gx[d] = gin[(gX + d) * cap + id];
+        for (int d = 0; d < 3; ++d) Gx[d] = gin[(gX + d) * cap + gi];
         if (mat == 4) {  // stationary: x' = x, v' = v, C' = C
 #pragma unroll
-          for (int d = 0; d < 3; ++d) gout[(gX + d) * cap + id] = Gx[d];
+          for (int d = 0; d < 3; ++d) gmid[d * cap + j] = Gx[d];
           active = false;
         } else {
-          const Base b = particle_base(P, st[kX * cap + j], st[(kX + 1) * cap + j], st[(kX + 2) * cap + j], bad);
+          const Base b = particle_base(P, cur[kX * cap + i], cur[(kX + 1) * cap + i], cur[(kX + 2) * cap + i], bad);
 #pragma unroll
           for (int d = 0; d < 3; ++d) {
             fx[d] = b.fx[d];
-            Gvt[d] = gin[(gV + d) * cap + id] + dt * Gx[d];  // x' = x + dt v'
+            Gvt[d] = gin[(gV + d) * cap + gi] + dt * Gx[d];  // x' = x + dt v'
           }
 #pragma unroll
-          for (int a = 0; a < 9; ++a) GC[a / 3][a % 3] = gin[(gC + a) * cap + id];
+          for (int a = 0; a < 9; ++a) GC[a / 3][a % 3] = gin[(gC + a) * cap + gi];
           bspline_weights(b.fx, wt);
           float dw[3][3];
           bspline_dweights(b.fx, dw);
@@ -226,7 +245,7 @@ __global__ __launch_bounds__(kAdjThreads) void k_g2p_adj(const MpmParams P, cons
                     gfx[cc] -= s4 * wgt * (GC[0][cc] * g[0] + GC[1][cc] * g[1] + GC[2][cc] * g[2]);
                 }
 #pragma unroll
-            for (int d = 0; d < 3; ++d) gout[(gX + d) * cap + id] = Gx[d] + P.inv_dx * gfx[d];
+            for (int d = 0; d < 3; ++d) gmid[d * cap + j] = Gx[d] + P.inv_dx * gfx[d];
           }
         }
       }
@@ -324,10 +343,11 @@ __global__ __launch_bounds__(256) void k_grid_adj(const MpmParams P, const Ws w,
 
 // ------------------------------------------------------------- P2G adj ----
 
+template <bool BY_ID>
 __global__ __launch_bounds__(kAdjThreads) void k_p2g_adj(const MpmParams P, const Ws w, const float *__restrict__ cur,
-                                                         const float *__restrict__ st, int64_t cap, float dt,
-                                                         const float *__restrict__ gin, float *__restrict__ gout,
-                                                         const float4 *__restrict__ ggrid, float *__restrict__ gE) {
+                                                         int64_t cap, float dt, const float *__restrict__ gin,
+                                                         const float *__restrict__ gmid, float *__restrict__ gout,
+                                                         const float4 *__restrict__ ggrid) {
   __shared__ float4 gt[kTileN];
   const int nitems = (int)min((int64_t)w.counters[2], w.items_cap);
   uint32_t bad = 0;
@@ -362,6 +382,12 @@ __global__ __launch_bounds__(kAdjThreads) void k_p2g_adj(const MpmParams P, cons
         bad |= MPM_STATUS_UNSUPPORTED;
         continue;
       }
+      if (BY_ID && (id < 0 || id >= cap)) {
+        bad |= MPM_STATUS_TABLE_OVERFLOW;
+        continue;
+      }
+      const int64_t gi = BY_ID ? id : (int64_t)j;  // column of gin
+      const int64_t go = BY_ID ? id : i;           // column of gout
       float x[3], v[3], C[3][3], F[3][3];
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
@@ -479,8 +505,8 @@ __global__ __launch_bounds__(kAdjThreads) void k_p2g_adj(const MpmParams P, cons
       // ---- reverse of the constitutive model ----
       float GFo[3][3];
 #pragma unroll
-      for (int a = 0; a < 9; ++a) GFo[a / 3][a % 3] = gin[(gF + a) * cap + id];
-      const float GJpo = gin[gJp * cap + id];
+      for (int a = 0; a < 9; ++a) GFo[a / 3][a % 3] = gin[(gF + a) * cap + gi];
+      const float GJpo = gin[gJp * cap + gi];
       float gFn[3][3];
       float gJ = la * (2.0f * J - 1.0f) * trgS;
       float gEv = 0.0f;
@@ -536,10 +562,10 @@ __global__ __launch_bounds__(kAdjThreads) void k_p2g_adj(const MpmParams P, cons
           cofactor(A, Ac);
           float detA = A[0][0] * Ac[0][0] + A[0][1] * Ac[0][1] + A[0][2] * Ac[0][2];
           if (fabsf(detA) < 1e-12f) detA = detA < 0.0f ? -1e-12f : 1e-12f;
-          const float id = 1.0f / detA;
+          const float inv_det = 1.0f / detA;
           float z[3];
 #pragma unroll
-          for (int r = 0; r < 3; ++r) z[r] = id * (Ac[0][r] * mv[0] + Ac[1][r] * mv[1] + Ac[2][r] * mv[2]);
+          for (int r = 0; r < 3; ++r) z[r] = inv_det * (Ac[0][r] * mv[0] + Ac[1][r] * mv[1] + Ac[2][r] * mv[2]);
           const float Zx[3][3] = {{0.0f, -z[2], z[1]}, {z[2], 0.0f, -z[0]}, {-z[1], z[0], 0.0f}};
 #pragma unroll
           for (int r = 0; r < 3; ++r)
@@ -597,23 +623,35 @@ __global__ __launch_bounds__(kAdjThreads) void k_p2g_adj(const MpmParams P, cons
           gFin[r][c] = acc;
         }
       if (mat == 0) gJp_out = gFin[0][0];
-      // ---- outputs (by particle id) ----
+      // ---- outputs: gradient of the state before the substep ----
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
-        gout[(gX + d) * cap + id] += P.inv_dx * gfx[d];
-        gout[(gV + d) * cap + id] = gv[d];
+        gout[(gX + d) * cap + go] = gmid[d * cap + j] + P.inv_dx * gfx[d];
+        gout[(gV + d) * cap + go] = gv[d];
       }
 #pragma unroll
       for (int a = 0; a < 9; ++a) {
-        gout[(gC + a) * cap + id] = gC_[a / 3][a % 3];
-        gout[(gF + a) * cap + id] = mat == 1 ? gFin[a / 3][a % 3] : 0.0f;
+        gout[(gC + a) * cap + go] = gC_[a / 3][a % 3];
+        gout[(gF + a) * cap + go] = mat == 1 ? gFin[a / 3][a % 3] : 0.0f;
       }
-      gout[gJp * cap + id] = gJp_out;
-      if (gE && perE) gE[id] += gEv;
+      gout[gJp * cap + go] = gJp_out;
+      gout[gE * cap + go] = gin[gE * cap + gi] + (perE ? gEv : 0.0f);  // E passes through the substep
     }
     __syncthreads();
   }
   set_status(w, bad);
+}
+
+// Gradient rows between original-id columns and the column order of a
+// particle state (its id row maps column j to an id).
+__global__ void k_grad_reorder(const float *__restrict__ st, int64_t cap, int64_t n, int rows,
+                               const float *__restrict__ src, float *__restrict__ dst, bool to_state_order) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const int64_t id = __float_as_int(st[kId * cap + j]);
+  if (id < 0 || id >= n) return;  // corrupted id row: leave the column untouched
+  const int64_t from = to_state_order ? id : j, to = to_state_order ? j : id;
+  for (int r = 0; r < rows; ++r) dst[r * cap + to] = src[r * cap + from];
 }
 
 }  // namespace mpm
@@ -646,14 +684,17 @@ int mpm_grid_snapshot(const MpmParams *p, void *ws, int64_t cap, float *keep, vo
   return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_E_CUDA;
 }
 
-int mpm_g2p_adj(const MpmParams *p, void *ws, int64_t cap, int64_t n, const float *st, float dt, const float *gin,
-                float *gout, float *ggrid, void *stream) {
-  if (!adj_params_ok(p) || !ws || !st || !gin || !gout || !ggrid || n < 0 || n > cap) return MPM_E_INVALID;
+int mpm_g2p_adj(const MpmParams *p, void *ws, int64_t cap, int64_t n, const float *cur, float dt, const float *gin,
+                float *gmid, float *ggrid, int32_t by_id, void *stream) {
+  if (!adj_params_ok(p) || !ws || !cur || !gin || !gmid || !ggrid || n < 0 || n > cap) return MPM_E_INVALID;
   const int sms = adj_dev_sms();
   if (!sms) return MPM_E_CUDA;
   Ws w;
   ws_layout(*p, cap, (char *)ws, &w);
-  k_g2p_adj<<<sms * 4, kAdjThreads, 0, (cudaStream_t)stream>>>(*p, w, st, cap, dt, gin, gout, (float4 *)ggrid);
+  if (by_id)
+    k_g2p_adj<true><<<sms * 4, kAdjThreads, 0, (cudaStream_t)stream>>>(*p, w, cur, cap, dt, gin, gmid, (float4 *)ggrid);
+  else
+    k_g2p_adj<false><<<sms * 4, kAdjThreads, 0, (cudaStream_t)stream>>>(*p, w, cur, cap, dt, gin, gmid, (float4 *)ggrid);
   return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_E_CUDA;
 }
 
@@ -668,15 +709,29 @@ int mpm_grid_adj(const MpmParams *p, void *ws, int64_t cap, const float *keep, f
   return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_E_CUDA;
 }
 
-int mpm_p2g_adj(const MpmParams *p, void *ws, int64_t cap, int64_t n, const float *cur, const float *st, float dt,
-                const float *gin, float *gout, const float *ggrid, float *gE, void *stream) {
-  if (!adj_params_ok(p) || !ws || !cur || !st || !gin || !gout || !ggrid || n < 0 || n > cap) return MPM_E_INVALID;
+int mpm_p2g_adj(const MpmParams *p, void *ws, int64_t cap, int64_t n, const float *cur, float dt, const float *gin,
+                const float *gmid, float *gout, const float *ggrid, int32_t by_id, void *stream) {
+  if (!adj_params_ok(p) || !ws || !cur || !gin || !gmid || !gout || !ggrid || gin == gout || n < 0 || n > cap)
+    return MPM_E_INVALID;
   const int sms = adj_dev_sms();
   if (!sms) return MPM_E_CUDA;
   Ws w;
   ws_layout(*p, cap, (char *)ws, &w);
-  k_p2g_adj<<<sms * 4, kAdjThreads, 0, (cudaStream_t)stream>>>(*p, w, cur, st, cap, dt, gin, gout,
-                                                               (const float4 *)ggrid, gE);
+  if (by_id)
+    k_p2g_adj<true><<<sms * 4, kAdjThreads, 0, (cudaStream_t)stream>>>(*p, w, cur, cap, dt, gin, gmid, gout,
+                                                                      (const float4 *)ggrid);
+  else
+    k_p2g_adj<false><<<sms * 4, kAdjThreads, 0, (cudaStream_t)stream>>>(*p, w, cur, cap, dt, gin, gmid, gout,
+                                                                       (const float4 *)ggrid);
+  return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_E_CUDA;
+}
+
+int mpm_grad_reorder(const float *state, int64_t cap, int64_t n, int32_t rows, const float *src, float *dst,
+                     int32_t to_state_order, void *stream) {
+  if (!state || !src || !dst || src == dst || n < 0 || n > cap || rows < 1 || rows > 64) return MPM_E_INVALID;
+  if (n == 0) return MPM_OK;
+  k_grad_reorder<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(state, cap, n, rows, src, dst,
+                                                                                to_state_order != 0);
   return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_E_CUDA;
 }
 

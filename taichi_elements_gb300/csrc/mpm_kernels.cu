@@ -820,6 +820,23 @@ int mpm_g2p(const MpmParams *p, void *ws, int64_t cap, int64_t n, float *nxt, fl
   return last_error();
 }
 
+int mpm_g2p_bin_into(const MpmParams *p, void *ws, void *ws_bins, int64_t cap, int64_t n, float *nxt, float dt,
+                     float *maxv_out, void *stream) {
+  if (!params_ok(p) || !ws || !ws_bins || !nxt || n < 0 || n > cap) return MPM_E_INVALID;
+  const DevInfo *di = dev_info();
+  if (!di) return MPM_E_CUDA;
+  Ws w, wb;
+  ws_layout(*p, cap, (char *)ws, &w);
+  ws_layout(*p, cap, (char *)ws_bins, &wb);
+  // the grid, sorted order and status stay with `ws`; only the next
+  // substep's cell counts, block flags and cell keys go to `ws_bins`
+  w.cell_cnt = wb.cell_cnt;
+  w.blk_flag = wb.blk_flag;
+  w.cellkey = wb.cellkey;
+  k_g2p<false><<<di->g2p_ctas, kG2PThreads, 0, (cudaStream_t)stream>>>(*p, nullptr, w, nxt, cap, dt, maxv_out);
+  return last_error();
+}
+
 int mpm_substep(const MpmParams *p, void *ws, int64_t cap, int64_t n, const float *cur, float *nxt, float dt,
                 float *maxv_out, void *stream) {
   int rc = mpm_bin_finalize(p, ws, cap, n, stream);

@@ -7,8 +7,10 @@ adjoint kernels of csrc/mpm_adjoint.cu substep by substep in reverse.  Memory
 is bounded by checkpointing: the full particle state is saved every
 `checkpoint_every` substeps during the forward pass; the backward pass
 recomputes one segment at a time from its checkpoint, keeping that segment's
-states, and then walks it backwards.  Gradients are carried in buffers
-indexed by original particle id.
+states (and, when memory allows, each substep's workspace), and then walks it
+backwards.  Inside a segment the gradient of each state is kept in that
+state's own sorted column order, so the adjoint kernels read and write it
+coalesced; between segments it is held by original particle id.
 
 Water and elastic particles are differentiated (snow and sand return maps are
 non-smooth and stay forward-only); a rollout containing other materials is
@@ -25,7 +27,8 @@ from . import _lib
 from ._lib import NROWS, ROW_C, ROW_EP, ROW_F, ROW_ID, ROW_JP, ROW_MAT, ROW_V, ROW_X
 from .mpm_solver import MPMSolver
 
-GROWS = 25  # dL/dx 3, dL/dv 3, dL/dC 9, dL/dF 9, dL/dJp 1
+GROWS = 26  # dL/dx 3, dL/dv 3, dL/dC 9, dL/dF 9, dL/dJp 1, dL/dE 1
+GROW_V, GROW_E = 3, 25
 
 
 class Rollout:
@@ -34,11 +37,12 @@ class Rollout:
     original particle id.
 
     Buffers are allocated once (checkpoints, one segment of states, two
-    gradient buffers), so each segment's forward, recomputation and adjoint
-    run as CUDA graphs after their first use."""
+    gradient buffers and, when memory allows, one workspace and grid-momentum
+    snapshot per substep of a segment), so each segment's forward,
+    recomputation and adjoint run as CUDA graphs after their first use."""
 
     def __init__(self, solver: MPMSolver, n_substeps: int, dt: float | None = None, checkpoint_every: int = 50,
-                 use_cuda_graph: bool = True):
+                 use_cuda_graph: bool = True, keep_workspaces: bool | None = None):
         if not solver.per_particle_E:
             raise ValueError("the differentiable rollout needs MPMSolver(per_particle_E=True)")
         self.s = solver
@@ -69,13 +73,28 @@ class Rollout:
         self.ring = torch.zeros((self.K, NROWS, self.cap), dtype=torch.float32, device=self.dev)
         self.tmp = torch.zeros_like(self.init)
         self.g = [torch.zeros((GROWS, self.cap), dtype=torch.float32, device=self.dev) for _ in range(2)]
-        self.gE = torch.zeros(self.cap, dtype=torch.float32, device=self.dev)
+        self.gid = torch.zeros((GROWS, self.cap), dtype=torch.float32, device=self.dev)  # by original id
+        self.gmid = torch.zeros((3, self.cap), dtype=torch.float32, device=self.dev)
         sp = ctypes.c_void_p(0)
         _lib.check(solver._lib.mpm_status_ptr(ctypes.byref(p), self.ws.data_ptr(), self.cap, ctypes.byref(sp)),
                    "status")
         off = sp.value - self.ws.data_ptr()
         self.status = self.ws[off:off + 4].view(torch.int32)
         self.status_acc = torch.zeros(1, dtype=torch.int32, device=self.dev)
+        self._status_off = off
+        # One workspace and one momentum snapshot per substep of a segment, so
+        # the recompute keeps what the adjoint needs (binning, sorted order,
+        # grid velocity, pre-update momentum) and the adjoint substep runs only
+        # its three kernels.  Without room for them the adjoint substep re-runs
+        # the forward binning, P2G and grid update into the single workspace.
+        per_slot = int(nbytes.value) + self.keep.numel() * 4
+        if keep_workspaces is None:
+            free, _ = torch.cuda.mem_get_info(self.dev)
+            keep_workspaces = self.K * per_slot <= free // 2
+        self.keep_workspaces = bool(keep_workspaces)
+        if self.keep_workspaces:
+            self.ws_ring = torch.zeros((self.K, int(nbytes.value)), dtype=torch.uint8, device=self.dev)
+            self.keep_ring = torch.zeros((self.K, nodes, 4), dtype=torch.float32, device=self.dev)
         self._graphs = {}
         self._seen = set()
 
@@ -98,8 +117,8 @@ class Rollout:
     def _collect_status(self):
         torch.bitwise_or(self.status_acc, self.status, out=self.status_acc)
 
-    def _check(self):
-        st = int(self.status_acc.item())
+    def _check(self, extra: int = 0):
+        st = int(self.status_acc.item()) | extra
         if st:
             self.status_acc.zero_()
             raise RuntimeError(f"MPM device status {st} in the differentiable rollout")
@@ -140,6 +159,8 @@ class Rollout:
 
     def _recompute_ops(self, count):
         """From self.a: ring[t] = state before substep t, t < count."""
+        if self.keep_workspaces:
+            return self._recompute_kept(count)
         self._reset_ws()
         self._bin(self.a)
         a, b = self.a, self.b
@@ -150,30 +171,66 @@ class Rollout:
         self._collect_status()
         self._reset_ws()
 
+    def _recompute_kept(self, count):
+        """From ring[0]: the forward of each substep t into its own workspace
+        ws_ring[t] (snapshot keep_ring[t]); G2P writes ring[t+1] and bins it
+        into ws_ring[t+1].  The last substep's G2P is not needed."""
+        cap, n, s, dt = self.cap, self.n, self.stream, self.dt
+        ws = [self.ws_ring[t].data_ptr() for t in range(count)]
+        self._call("mpm_bin_count", ws[0], cap, self.ring[0].data_ptr(), 0, n, s)
+        for t in range(count):
+            cur = self.ring[t]
+            nxt = self.ring[t + 1] if t + 1 < count else self.b
+            self._call("mpm_bin_finalize", ws[t], cap, n, s)
+            self._call("mpm_p2g", ws[t], cap, n, cur.data_ptr(), nxt.data_ptr(), dt, s)
+            self._call("mpm_grid_snapshot", ws[t], cap, self.keep_ring[t].data_ptr(), s)
+            self._call("mpm_grid_update", ws[t], cap, dt, s)
+            if t + 1 < count:
+                self._call("mpm_g2p_bin_into", ws[t], ws[t + 1], cap, n, nxt.data_ptr(), dt, None, s)
+
     def _adjoint_ops(self, count):
-        """Walk ring[count-1 .. 0] backwards; gradient stays in self.g[0]."""
+        """Walk ring[count-1 .. 0] backwards, from the gradient in self.gid
+        (by id, with respect to the state after the segment) to the gradient
+        with respect to the segment's first state, written back to self.gid."""
         gin, gout = self.g
+        n, cap, s = self.n, self.cap, self.stream
+        if self.keep_workspaces:  # columns in the order of the recomputed end state
+            _lib.check(self.s._lib.mpm_grad_reorder(self.b.data_ptr(), cap, n, GROWS, self.gid.data_ptr(),
+                                                    gin.data_ptr(), 1, s), "mpm_grad_reorder")
+        else:
+            gin.copy_(self.gid)
         for t in reversed(range(count)):
-            self._adjoint_substep(self.ring[t], gin, gout)
+            if self.keep_workspaces:
+                self._adjoint_kernels(self.ws_ring[t].data_ptr(), self.keep_ring[t], self.ring[t], gin, gout, 0)
+            else:
+                self._adjoint_substep(self.ring[t], gin, gout)
             gin, gout = gout, gin
-        if count % 2:
-            self.g[0].copy_(self.g[1])
-        self._collect_status()
+        if self.keep_workspaces:
+            _lib.check(self.s._lib.mpm_grad_reorder(self.ring[0].data_ptr(), cap, n, GROWS, gin.data_ptr(),
+                                                    self.gid.data_ptr(), 0, s), "mpm_grad_reorder")
+        else:
+            self.gid.copy_(gin)
+            self._collect_status()
+
+    def _adjoint_kernels(self, ws, keep, cur, gin, gout, by_id):
+        cap, n, s, dt = self.cap, self.n, self.stream, self.dt
+        self.ggrid.zero_()
+        self._call("mpm_g2p_adj", ws, cap, n, cur.data_ptr(), dt, gin.data_ptr(), self.gmid.data_ptr(),
+                   self.ggrid.data_ptr(), by_id, s)
+        self._call("mpm_grid_adj", ws, cap, keep.data_ptr(), self.ggrid.data_ptr(), dt, s)
+        self._call("mpm_p2g_adj", ws, cap, n, cur.data_ptr(), dt, gin.data_ptr(), self.gmid.data_ptr(),
+                   gout.data_ptr(), self.ggrid.data_ptr(), by_id, s)
 
     def _adjoint_substep(self, cur, gin, gout):
-        ws, cap, n, s = self.ws.data_ptr(), self.cap, self.n, self.stream
-        dt = self.dt
+        """Re-run the forward of the substep from `cur` into the single
+        workspace, then its adjoint (gradients by original id)."""
+        ws, cap, n, s, dt = self.ws.data_ptr(), self.cap, self.n, self.stream, self.dt
         self._bin(cur)
         self._call("mpm_bin_finalize", ws, cap, n, s)
         self._call("mpm_p2g", ws, cap, n, cur.data_ptr(), self.tmp.data_ptr(), dt, s)
         self._call("mpm_grid_snapshot", ws, cap, self.keep.data_ptr(), s)
         self._call("mpm_grid_update", ws, cap, dt, s)
-        self.ggrid.zero_()
-        self._call("mpm_g2p_adj", ws, cap, n, self.tmp.data_ptr(), dt, gin.data_ptr(), gout.data_ptr(),
-                   self.ggrid.data_ptr(), s)
-        self._call("mpm_grid_adj", ws, cap, self.keep.data_ptr(), self.ggrid.data_ptr(), dt, s)
-        self._call("mpm_p2g_adj", ws, cap, n, cur.data_ptr(), self.tmp.data_ptr(), dt, gin.data_ptr(),
-                   gout.data_ptr(), self.ggrid.data_ptr(), self.gE.data_ptr(), s)
+        self._adjoint_kernels(ws, self.keep, cur, gin, gout, 1)
 
     # ------------------------------------------------------------- forward --
 
@@ -215,18 +272,25 @@ class Rollout:
     def backward(self, gx_final: torch.Tensor):
         """dL/dv0 (n,3) and dL/dE (n,) by particle id, given dL/dx_final."""
         n = self.n
-        for g in self.g:
-            g.zero_()
-        self.g[0][0:3, :n] = gx_final.to(self.dev, torch.float32).t()
-        self.gE.zero_()
+        self.gid.zero_()
+        self.gid[0:3, :n] = gx_final.to(self.dev, torch.float32).t()
+        if self.keep_workspaces:
+            # each workspace's cell counts and block flags return to zero when
+            # its substep runs, so one clear per backward pass suffices
+            self.ws_ring.zero_()
         for seg in reversed(range(self.nseg)):
             count = self._seg_len(seg)
-            self.a.copy_(self.ckpt[seg])
+            (self.ring[0] if self.keep_workspaces else self.a).copy_(self.ckpt[seg])
             self._graphed("rec", count, self._recompute_ops)
             self._graphed("adj", count, self._adjoint_ops)
         torch.cuda.synchronize()
-        self._check()
-        return self.g[0][3:6, :n].t().contiguous(), self.gE[:n].clone()
+        extra = 0
+        if self.keep_workspaces:
+            off = self._status_off
+            for v in self.ws_ring[:, off:off + 4].view(torch.int32).reshape(-1).tolist():
+                extra |= v
+        self._check(extra)
+        return self.gid[GROW_V:GROW_V + 3, :n].t().contiguous(), self.gid[GROW_E, :n].clone()
 
 
 class _RolloutFunction(torch.autograd.Function):

@@ -137,13 +137,56 @@ __global__ __launch_bounds__(256) void k_grid_snapshot(const MpmParams P, const 
 
 // ------------------------------------------------------------- G2P adj ----
 
+// One pass of the G2P-adjoint stencil of a warp's particles over the 27
+// nodes: every lane adds w (Gvt + s4 GC (off - fx)) into its warp tile (the
+// store is predicated on `mine`, the lanes of this pass hold distinct
+// cells); with GATHER (first pass) it also accumulates dL/dfx from the grid
+// velocities `vt` through the weights and through (off - fx).
+template <bool GATHER>
+__device__ __forceinline__ void g2p_adj_nodes(float4 *tile, const float4 *vt, int base_node, bool mine,
+                                              const float (&wt)[3][3], const float (&dw)[3][3], const float (&fx)[3],
+                                              const float (&Gvt)[3], const float (&GC)[3][3], float s4,
+                                              float (&gfx)[3]) {
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int bb = 0; bb < 3; ++bb)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const int node = base_node + (a * kTileW + bb) * kTileW + c;
+        const float d[3] = {(float)a - fx[0], (float)bb - fx[1], (float)c - fx[2]};
+        const float wgt = wt[a][0] * wt[bb][1] * wt[c][2];
+        float q[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) q[r] = Gvt[r] + s4 * (GC[r][0] * d[0] + GC[r][1] * d[1] + GC[r][2] * d[2]);
+        // unconditional read and arithmetic, predicated store only
+        float4 *nd = tile + node;
+        float4 g = *nd;
+        g.x += wgt * q[0];
+        g.y += wgt * q[1];
+        g.z += wgt * q[2];
+        if (mine) *nd = g;
+        __syncwarp();
+        if constexpr (GATHER) {
+          const float4 v4 = vt[node];
+          const float gw = v4.x * q[0] + v4.y * q[1] + v4.z * q[2];
+          gfx[0] += gw * dw[a][0] * wt[bb][1] * wt[c][2];
+          gfx[1] += gw * wt[a][0] * dw[bb][1] * wt[c][2];
+          gfx[2] += gw * wt[a][0] * wt[bb][1] * dw[c][2];
+#pragma unroll
+          for (int cc = 0; cc < 3; ++cc)
+            gfx[cc] -= s4 * wgt * (GC[0][cc] * v4.x + GC[1][cc] * v4.y + GC[2][cc] * v4.z);
+        }
+      }
+}
+
 // Gradient indexing: with BY_ID, gradient columns are original particle ids;
 // otherwise `gin` is in the order of the sorted substep output (column j)
 // and `gout` in the order of the substep input `cur` (column pid[j]).  The
 // position part of dL/dx from G2P goes to `gmid` (3 rows, column j) and is
 // added into `gout` by k_p2g_adj.
 template <bool BY_ID>
-__global__ __launch_bounds__(kAdjThreads) void k_g2p_adj(const MpmParams P, const Ws w, const float *__restrict__ cur,
+__global__ __launch_bounds__(kAdjThreads, 4) void k_g2p_adj(const MpmParams P, const Ws w, const float *__restrict__ cur,
                                                          int64_t cap, float dt, const float *__restrict__ gin,
                                                          float *__restrict__ gmid, float4 *__restrict__ ggrid) {
   __shared__ float4 vt[kTileN];
@@ -175,7 +218,8 @@ __global__ __launch_bounds__(kAdjThreads) void k_g2p_adj(const MpmParams P, cons
       int cell = -1 - lane;
       int lx = 0, ly = 0, lz = 0;
       float wt[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
-      float fx[3] = {0.f, 0.f, 0.f}, Gvt[3] = {0.f, 0.f, 0.f}, GC[3][3];
+      float dw[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+      float fx[3] = {0.f, 0.f, 0.f}, Gvt[3] = {0.f, 0.f, 0.f}, Gx[3] = {0.f, 0.f, 0.f}, GC[3][3];
 #pragma unroll
       for (int a = 0; a < 9; ++a) GC[a / 3][a % 3] = 0.0f;
       const int64_t i = active ? (int64_t)w.pid[j] : 0;
@@ -190,7 +234,6 @@ __global__ __launch_bounds__(kAdjThreads) void k_g2p_adj(const MpmParams P, cons
       }
       if (active) {
         const int mat = __float_as_int(cur[kMat * cap + i]) & 0xFF;
-        float Gx[3];
 #pragma unroll
         for (int d = 0; d < 3; ++d) Gx[d] = gin[(gX + d) * cap + gi];
         if (mat == 4) {  // stationary: x' = x, v' = v, C' = C
@@ -199,16 +242,6 @@ __global__ __launch_bounds__(kAdjThreads) void k_g2p_adj(const MpmParams P, cons
           active = false;
         } else {
           const Base b = particle_base(P, cur[kX * cap + i], cur[(kX + 1) * cap + i], cur[(kX + 2) * cap + i], bad);
-#pragma unroll
-          for (int d = 0; d < 3; ++d) {
-            fx[d] = b.fx[d];
-            Gvt[d] = gin[(gV + d) * cap + gi] + dt * Gx[d];  // x' = x + dt v'
-          }
-#pragma unroll
-          for (int a = 0; a < 9; ++a) GC[a / 3][a % 3] = gin[(gC + a) * cap + gi];
-          bspline_weights(b.fx, wt);
-          float dw[3][3];
-          bspline_dweights(b.fx, dw);
           lx = b.b[0] - bx * 4;
           ly = b.b[1] - by * 4;
           lz = b.b[2] - bz * 4;
@@ -217,63 +250,33 @@ __global__ __launch_bounds__(kAdjThreads) void k_g2p_adj(const MpmParams P, cons
             active = false;
             lx = ly = lz = 0;
           } else {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+              fx[d] = b.fx[d];
+              Gvt[d] = gin[(gV + d) * cap + gi] + dt * Gx[d];  // x' = x + dt v'
+            }
+#pragma unroll
+            for (int a = 0; a < 9; ++a) GC[a / 3][a % 3] = gin[(gC + a) * cap + gi];
+            bspline_weights(b.fx, wt);
+            bspline_dweights(b.fx, dw);
             cell = local_cell(lx, ly, lz);
-            // dL/dfx through the weights and through (off - fx)
-            float gfx[3] = {0.f, 0.f, 0.f};
-            const int base_node = (lx * kTileW + ly) * kTileW + lz;
-#pragma unroll
-            for (int a = 0; a < 3; ++a)
-#pragma unroll
-              for (int bb = 0; bb < 3; ++bb)
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                  const float4 g4 = vt[base_node + (a * kTileW + bb) * kTileW + c];
-                  const float g[3] = {g4.x, g4.y, g4.z};
-                  const float d[3] = {(float)a - fx[0], (float)bb - fx[1], (float)c - fx[2]};
-                  const float wgt = wt[a][0] * wt[bb][1] * wt[c][2];
-                  float gw = 0.0f;
-#pragma unroll
-                  for (int r = 0; r < 3; ++r) {
-                    const float GCd = GC[r][0] * d[0] + GC[r][1] * d[1] + GC[r][2] * d[2];
-                    gw += g[r] * (Gvt[r] + s4 * GCd);
-                  }
-                  gfx[0] += gw * dw[a][0] * wt[bb][1] * wt[c][2];
-                  gfx[1] += gw * wt[a][0] * dw[bb][1] * wt[c][2];
-                  gfx[2] += gw * wt[a][0] * wt[bb][1] * dw[c][2];
-#pragma unroll
-                  for (int cc = 0; cc < 3; ++cc)
-                    gfx[cc] -= s4 * wgt * (GC[0][cc] * g[0] + GC[1][cc] * g[1] + GC[2][cc] * g[2]);
-                }
-#pragma unroll
-            for (int d = 0; d < 3; ++d) gmid[d * cap + j] = Gx[d] + P.inv_dx * gfx[d];
           }
         }
       }
-      // grid-velocity gradients: g(v_i) += w (Gvt + s4 GC (off - fx))
+      // grid-velocity gradients g(v_i) += w (Gvt + s4 GC (off - fx)), one
+      // pass per set of lanes with distinct cells; the first pass also
+      // gathers dL/dfx
       const unsigned peers = __match_any_sync(0xffffffffu, cell);
       const int round_of_lane = __popc(peers & ((1u << lane) - 1u));
-      for (int round = 0;; ++round) {
-        const bool mine = active && round_of_lane == round;
-        const int base_node = (lx * kTileW + ly) * kTileW + lz;
+      const int base_node = (lx * kTileW + ly) * kTileW + lz;
+      float gfx[3] = {0.f, 0.f, 0.f};
+      g2p_adj_nodes<true>(tile, vt, base_node, active && round_of_lane == 0, wt, dw, fx, Gvt, GC, s4, gfx);
+      if (active) {
 #pragma unroll
-        for (int a = 0; a < 3; ++a)
-#pragma unroll
-          for (int bb = 0; bb < 3; ++bb)
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-              // unconditional read and arithmetic, predicated store only
-              const float d[3] = {(float)a - fx[0], (float)bb - fx[1], (float)c - fx[2]};
-              const float wgt = wt[a][0] * wt[bb][1] * wt[c][2];
-              float4 *nd = tile + base_node + (a * kTileW + bb) * kTileW + c;
-              float4 g = *nd;
-              g.x += wgt * (Gvt[0] + s4 * (GC[0][0] * d[0] + GC[0][1] * d[1] + GC[0][2] * d[2]));
-              g.y += wgt * (Gvt[1] + s4 * (GC[1][0] * d[0] + GC[1][1] * d[1] + GC[1][2] * d[2]));
-              g.z += wgt * (Gvt[2] + s4 * (GC[2][0] * d[0] + GC[2][1] * d[1] + GC[2][2] * d[2]));
-              if (mine) *nd = g;
-              __syncwarp();
-            }
-        if (!__any_sync(0xffffffffu, active && round_of_lane > round)) break;
+        for (int d = 0; d < 3; ++d) gmid[d * cap + j] = Gx[d] + P.inv_dx * gfx[d];
       }
+      for (int round = 1; __any_sync(0xffffffffu, active && round_of_lane >= round); ++round)
+        g2p_adj_nodes<false>(tile, vt, base_node, active && round_of_lane == round, wt, dw, fx, Gvt, GC, s4, gfx);
     }
     __syncthreads();
     for (int t = threadIdx.x; t < kTileN; t += blockDim.x) {
@@ -344,7 +347,7 @@ __global__ __launch_bounds__(256) void k_grid_adj(const MpmParams P, const Ws w,
 // ------------------------------------------------------------- P2G adj ----
 
 template <bool BY_ID>
-__global__ __launch_bounds__(kAdjThreads) void k_p2g_adj(const MpmParams P, const Ws w, const float *__restrict__ cur,
+__global__ __launch_bounds__(kAdjThreads, 4) void k_p2g_adj(const MpmParams P, const Ws w, const float *__restrict__ cur,
                                                          int64_t cap, float dt, const float *__restrict__ gin,
                                                          const float *__restrict__ gmid, float *__restrict__ gout,
                                                          const float4 *__restrict__ ggrid) {

@@ -144,13 +144,22 @@ def barrier(ws):
 
 
 def allmax(x, ws):
+    """Maximum of a per-rank float over all ranks (the slowest replica's
+    time); a CPU tensor when the process group runs on gloo."""
     if ws == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_value(units_per_rank, steps, ws, total_ms):
+    """Whole-job throughput of N independent replicas: the units all ranks
+    processed divided by the slowest rank's time (max over ranks)."""
+    return units_per_rank * steps * ws / (total_ms / 1e3)
 
 
 def p2g_traffic(n_particles):
@@ -245,7 +254,7 @@ def run_gb300(args):
     ph = np.array([[e[i].elapsed_time(e[i + 1]) for i in range(4)] for e in evs])
     ph_mean = ph.mean(0)
     n = solver.n_particles
-    value = n * args.steps * ws / (total_ms / 1e3)
+    value = replica_value(n, args.steps, ws, total_ms)
     peak, peak_kind = load_peaks()
     p2g_bytes = P2G_BYTES_PER_PARTICLE * n + P2G_BYTES_PER_NODE * n_nodes
     p2g_ach = p2g_bytes / (ph_mean[1] / 1e3) / 1e9

@@ -1,12 +1,17 @@
 """Gradients of a final-state loss through a GPU rollout (float32 forward,
 hand-written adjoint, checkpointed segments) against two float64
 references: PyTorch autograd through oracle/torch_ref.py, and central
-finite differences of the C oracle along random directions.
+finite differences of the C oracle along 10 random directions each for the
+initial velocities and for E.  Case: the differentiable scene's small copy,
+a 32^3 grid with 2,000 water + 2,000 elastic particles, 200 substeps,
+checkpoints every 50.
 
 Tolerance: relative L2 error of dL/dv0 and dL/dE against the float64
-autograd gradient <= 3e-2, and each directional derivative within 3e-2 of
-the finite difference (relative to the gradient's norm times the direction's
-norm); float32 round-off over the rollout sets this bound.
+autograd gradient <= 1e-3, and each directional derivative within 2e-3 of
+the finite difference (relative to the larger of |FD| and the gradient's
+norm times the direction's RMS); float32 round-off over the rollout sets
+this bound (measured on a GB300: 4e-7 and 9e-6 against autograd, <= 2e-4
+against FD).
 """
 import numpy as np
 import pytest
@@ -18,12 +23,13 @@ from taichi_elements_gb300 import scenes
 
 pytestmark = pytest.mark.gpu
 
-NSUB = 48
-K = 16
+NSUB = 200
+K = 50
+NDIR = 10
 
 
-def make_case(seed=3):
-    sc = scenes.elastic_on_water(res=32, n_each=1200)
+def make_case(seed=3, n_each=2000):
+    sc = scenes.elastic_on_water(res=32, n_each=n_each)
     rng = np.random.default_rng(seed)
     n = sc.n
     v0 = (sc.v + rng.normal(0.0, 0.3, (n, 3))).astype(np.float32)
@@ -71,8 +77,10 @@ def test_adjoint_matches_float64_autograd():
     assert abs(Lg - Lr) <= 1e-3 * abs(Lr) + 1e-9
     ev = np.linalg.norm(gv - gv_r) / np.linalg.norm(gv_r)
     eE = np.linalg.norm(gE - gE_r) / np.linalg.norm(gE_r)
-    assert ev < 3e-2, ev
-    assert eE < 3e-2, eE
+    print(f"adjoint vs float64 autograd: x {np.abs(xg - xr).max():.2e}, L {abs(Lg - Lr) / abs(Lr):.2e}, "
+          f"dL/dv0 {ev:.2e}, dL/dE {eE:.2e}")
+    assert ev < 1e-3, ev
+    assert eE < 1e-3, eE
 
 
 def test_adjoint_directional_derivatives_match_finite_differences():
@@ -92,16 +100,18 @@ def test_adjoint_directional_derivatives_match_finite_differences():
 
     def close(gd, fd, g, d):
         scale = np.linalg.norm(g) * np.linalg.norm(d) / np.sqrt(d.size)  # typical |<g, d>|
-        return abs(gd - fd) <= 3e-2 * max(abs(fd), scale)
+        return abs(gd - fd) <= 2e-3 * max(abs(fd), scale)
 
-    for _ in range(3):
+    for _ in range(NDIR):
         d = rng.standard_normal(v0.shape)
         h = 1e-4
         fd = (loss(v0d + h * d, Ed) - loss(v0d - h * d, Ed)) / (2 * h)
+        print(f"FD v0 direction: adjoint {(gv * d).sum():.6e} fd {fd:.6e}")
         assert close((gv * d).sum(), fd, gv, d), ((gv * d).sum(), fd)
         dE = rng.standard_normal(E.shape) * Ed
         hE = 1e-4
         fdE = (loss(v0d, Ed + hE * dE) - loss(v0d, Ed - hE * dE)) / (2 * hE)
+        print(f"FD E direction: adjoint {(gE * dE).sum():.6e} fd {fdE:.6e}")
         assert close((gE * dE).sum(), fdE, gE * Ed, dE / Ed), ((gE * dE).sum(), fdE)
 
 
@@ -110,7 +120,7 @@ def test_adjoint_with_and_without_kept_workspaces_agree():
     re-runs each substep's forward before its adjoint give the same
     gradients (up to the order of float atomics); 40 substeps in segments of
     16, 16 and 8."""
-    sc, v0, E = make_case(seed=5)
+    sc, v0, E = make_case(seed=5, n_each=1200)
     a = gpu_grads(sc, v0, E, nsub=40, k=16, keep_workspaces=True)
     b = gpu_grads(sc, v0, E, nsub=40, k=16, keep_workspaces=False)
     assert np.abs(a[1] - b[1]).max() < 1e-5

@@ -6,8 +6,8 @@ the constructor (:44-310), the material/surface constants (:16-42),
 (:1097-1104), ``read_restart`` (:1128-1144), ``add_surface_collider``
 (:647-687), ``add_sphere_collider`` (:618-642), ``add_bounding_box``
 (:689-692), ``clear_grid_postprocess`` (:644-645), ``set_gravity``
-(:316-319), ``step`` (:748-821), ``particle_info`` (:1172-1191) and
-``clear_particles`` (:1193-1196).
+(:316-319), ``set_source_velocity`` (:852-859), ``step`` (:748-821),
+``particle_info`` (:1172-1191) and ``clear_particles`` (:1193-1196).
 
 State lives in PyTorch CUDA tensors; every substep runs the hand-written
 sm_103a kernels of libmpm_gb300.so through ctypes.  There is no CPU path: a
@@ -160,6 +160,7 @@ class MPMSolver:
         self.autotune = bool(autotune)
         self._tuned = False
         self.gravity = (0.0, -9.8, 0.0)
+        self.source_velocity = (0.0, 0.0, 0.0)
         self.grid_postprocess = []  # records: dicts with kind/surface/...
         self.add_bounding_box(self.unbounded)
 
@@ -252,6 +253,17 @@ class MPMSolver:
         assert len(g) == self.dim
         self.gravity = tuple(float(x) for x in g)
         self._invalidate_params()
+
+    def set_source_velocity(self, velocity):
+        """engine/mpm_solver.py:852-859: the velocity the seeding routines
+        give new particles (None = zero).  Each add_* call sets it from its
+        own `velocity` argument, as in the reference."""
+        if velocity is not None:
+            velocity = list(velocity)
+            assert len(velocity) == self.dim
+            self.source_velocity = tuple(float(v) for v in velocity)
+        else:
+            self.source_velocity = (0.0,) * self.dim
 
     # -------------------------------------------------------- colliders ---
 
@@ -375,8 +387,8 @@ class MPMSolver:
         if isinstance(velocity, torch.Tensor):
             s[ROW_V:ROW_V + 3, a:b] = velocity.to(self.device, torch.float32).t()
         else:
-            vel = [0.0, 0.0, 0.0] if velocity is None else list(velocity)
-            assert len(vel) == self.dim
+            self.set_source_velocity(velocity)
+            vel = list(self.source_velocity)
             for d in range(3):
                 s[ROW_V + d, a:b] = float(np.float32(vel[d]))
         s[ROW_C:ROW_C + 9, a:b] = 0.0

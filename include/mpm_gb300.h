@@ -240,6 +240,25 @@ int mpm_substep_noalloc(const MpmParams *p, int64_t cap, int64_t n, const float 
 int mpm_gather_rows(const float *pstate, int64_t cap, int64_t n, int32_t row0, int32_t ncols,
                     float *out, void *stream);
 
+/* ---- Particle output (engine/particle_io.py:12-76, ParticleIO.write_particles)
+ * The quantised frame format: per dimension, positions and velocities are
+ * mapped to their [min, max] range over all particles (max raised to
+ * min + 1e-5 when narrower, :48-50), quantised to 24 and 8 bits with the
+ * reference's float32 expression and packed into one uint32 per component,
+ * (qx << 8) + qv (uint32 wrap-around).
+ * mpm_particle_ranges: `keys` is a device uint32[12] scratch, `ranges_out` a
+ *   device float[12] laid out as the reference's (2, 3, 2) `ranges` array
+ *   (positions then velocities; per dimension min, max).  n >= 1.
+ * mpm_quantize_particles: `x_and_v` is a device uint32[n * 3] in ORIGINAL
+ *   particle order (rows scattered by the id row of `pstate`).
+ * mpm_unpack_colors: 24-bit colours (device int32[n], original order) to a
+ *   device uint8[n * 3] of R, G, B (:62-74). */
+int mpm_particle_ranges(const float *pstate, int64_t cap, int64_t n, uint32_t *keys, float *ranges_out,
+                        void *stream);
+int mpm_quantize_particles(const float *pstate, int64_t cap, int64_t n, const float *ranges, uint32_t *x_and_v,
+                           void *stream);
+int mpm_unpack_colors(const int32_t *color, int64_t n, uint8_t *rgb, void *stream);
+
 /* Pointer to the device status word inside the workspace (uint32). */
 int mpm_status_ptr(const MpmParams *p, void *ws, int64_t cap, uint32_t **status_out);
 

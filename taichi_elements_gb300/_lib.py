@@ -108,6 +108,9 @@ SIGNATURES = {
     "mpm_grid_snapshot": [_P, _v, _i64, _v, _v],
     "mpm_g2p_bin_into": [_P, _v, _v, _i64, _i64, _v, _f, _v, _v],
     "mpm_grad_reorder": [_v, _i64, _i64, _i32, _v, _v, _i32, _v],
+    "mpm_particle_ranges": [_v, _i64, _i64, _v, _v, _v],
+    "mpm_quantize_particles": [_v, _i64, _i64, _v, _v, _v],
+    "mpm_unpack_colors": [_v, _i64, _v, _v],
     "mpm_g2p_adj": [_P, _v, _i64, _i64, _v, _f, _v, _v, _v, _i32, _v],
     "mpm_grid_adj": [_P, _v, _i64, _v, _v, _f, _v],
     "mpm_p2g_adj": [_P, _v, _i64, _i64, _v, _f, _v, _v, _v, _v, _i32, _v],

@@ -7,7 +7,8 @@ the constructor (:44-310), the material/surface constants (:16-42),
 (:647-687), ``add_sphere_collider`` (:618-642), ``add_bounding_box``
 (:689-692), ``clear_grid_postprocess`` (:644-645), ``set_gravity``
 (:316-319), ``set_source_velocity`` (:852-859), ``step`` (:748-821),
-``particle_info`` (:1172-1191) and ``clear_particles`` (:1193-1196).
+``particle_info`` (:1172-1191), ``clear_particles`` (:1193-1196) and the
+frame writers ``write_particles`` / ``write_particles_ply`` (:1198-1209).
 
 State lives in PyTorch CUDA tensors; every substep runs the hand-written
 sm_103a kernels of libmpm_gb300.so through ctypes.  There is no CPU path: a
@@ -751,4 +752,13 @@ class MPMSolver:
         }
 
     def write_particles(self, fn, slice_size=1000000):
-        raise NotImplementedError("particle file output is not part of the GB300 engine")
+        """engine/mpm_solver.py:1198-1200: the quantised .npz frame of
+        engine/particle_io.py, quantised on the GPU."""
+        from .particle_io import ParticleIO
+        ParticleIO.write_particles(self, fn, slice_size)
+
+    def write_particles_ply(self, fn):
+        """engine/mpm_solver.py:1202-1209: positions and colours as a
+        binary point-cloud .ply."""
+        from .particle_io import write_particles_ply
+        write_particles_ply(self, fn)

@@ -272,6 +272,9 @@ def run_gb300(args):
     adjoint = None
     if not args.no_adjoint:
         adjoint = run_adjoint_measure()
+    pio = None
+    if not args.no_io:
+        pio = run_particle_output_measure(solver, peak, peak_kind, rank == 0 and not args.no_cpu)
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(sc, args)
@@ -313,6 +316,7 @@ def run_gb300(args):
         "cpu_baseline": cpu,
         "batched": batched,
         "fwd_adjoint": adjoint,
+        "particle_output": pio,
     }
     if rank == 0:
         print(json.dumps(line))
@@ -356,6 +360,71 @@ def run_e2e(sc, args, ws):
             "step": f"one step(frame_dt) frame of {count} substeps + particle_info(); read_restart of the scene "
                     f"from pinned host memory inside the timed region (amortised over {frames} frames)",
             "frames": frames, "seconds": t}
+
+
+# algorithmic bytes per particle of one quantised frame: the range pass reads
+# x, v (24); quantisation reads x, v, id (28) and writes x_and_v (12); the
+# colour pass reads 4 and writes 3
+IO_BYTES_PER_PARTICLE = 24 + 28 + 12 + 7
+
+
+def run_particle_output_measure(solver, peak, peak_kind, with_cpu, reps=20):
+    """The reference's quantised frame (engine/particle_io.py:12-76) of the
+    bench scene: the three device kernels timed with CUDA events, the frame
+    to host numpy arrays end to end, and the CPU restatement on a sample."""
+    import torch
+
+    from taichi_elements_gb300._lib import ROW_V, ROW_X
+    from taichi_elements_gb300.particle_io import ParticleIO
+    n, lib, s = solver.n_particles, solver._lib, solver.stream
+    st = solver._state[solver._cur]
+    keys = torch.empty(12, dtype=torch.int32, device="cuda")
+    ranges = torch.empty(12, dtype=torch.float32, device="cuda")
+    xv = torch.empty((n, 3), dtype=torch.int32, device="cuda")
+    rgb = torch.empty((n, 3), dtype=torch.uint8, device="cuda")
+
+    def kernels():
+        lib.mpm_particle_ranges(st.data_ptr(), solver._cap, n, keys.data_ptr(), ranges.data_ptr(), s)
+        lib.mpm_quantize_particles(st.data_ptr(), solver._cap, n, ranges.data_ptr(), xv.data_ptr(), s)
+        lib.mpm_unpack_colors(solver._color.data_ptr(), n, rgb.data_ptr(), s)
+
+    for _ in range(3):
+        kernels()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        kernels()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    ach = IO_BYTES_PER_PARTICLE * n / (ms / 1e3) / 1e9
+    ParticleIO.quantize(solver)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ParticleIO.quantize(solver)
+    t_e2e = time.perf_counter() - t0
+    out = {"value": n / (ms / 1e3), "unit": "particles/s (quantised frame, device kernels)",
+           "ms_per_frame": ms, "particles": n,
+           "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                        "algorithmic_bytes_per_particle": IO_BYTES_PER_PARTICLE, "peak_source": peak_kind},
+           "e2e": {"value": n / t_e2e, "unit": "particles/s (device state to host numpy frame arrays)",
+                   "d2h_bytes": 15 * n + 48},
+           "gpu_launches_per_frame": 5}
+    if with_cpu:
+        from oracle import particle_io_ref as R
+        m = min(n, 2_000_000)
+        x = solver._gather(ROW_X, 3)[:m].cpu().numpy()
+        v = solver._gather(ROW_V, 3)[:m].cpu().numpy()
+        col = solver._color[:m].cpu().numpy()
+        t0 = time.perf_counter()
+        R.write_arrays(x, v, col)
+        tc = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": m / tc, "unit": "particles/s", "cores": 1, "kind": "port",
+                               "sample": f"{m} particles of the scene through the numpy restatement of "
+                                         "ParticleIO.write_particles (the reference's own code is numpy)"}
+    return out
 
 
 def run_batched_measure(frames=3, substeps=50):
@@ -538,6 +607,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-io", action="store_true", help="skip the particle-output measurement")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--e2e-frames", type=int, default=3)
     ap.add_argument("--e2e-substeps", type=int, default=50)

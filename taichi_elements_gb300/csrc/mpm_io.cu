@@ -91,6 +91,15 @@ __device__ __forceinline__ uint32_t quantise(float v, float lo, float inv, float
 __global__ __launch_bounds__(kIoThreads) void k_quantise(const float *__restrict__ st, int64_t cap, int64_t n,
                                                          const float *__restrict__ ranges,
                                                          uint32_t *__restrict__ out) {
+  // per range: lo and 1 / (hi - lo), computed once per CTA (the reference
+  // computes the reciprocal once per dimension, engine/particle_io.py:51-56)
+  __shared__ float lo_s[6], inv_s[6];
+  if (threadIdx.x < 6) {
+    const float lo = ranges[2 * threadIdx.x], hi = ranges[2 * threadIdx.x + 1];
+    lo_s[threadIdx.x] = lo;
+    inv_s[threadIdx.x] = __fdiv_rn(1.0f, __fsub_rn(hi, lo));
+  }
+  __syncthreads();
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
   const int64_t id = __float_as_int(st[kId * cap + j]);
@@ -98,12 +107,8 @@ __global__ __launch_bounds__(kIoThreads) void k_quantise(const float *__restrict
   const float xs = (float)((1u << kXBits) - 1u), vs = (float)((1u << kVBits) - 1u);
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    const float xlo = ranges[d * 2], xhi = ranges[d * 2 + 1];
-    const float vlo = ranges[6 + d * 2], vhi = ranges[6 + d * 2 + 1];
-    const float xinv = __fdiv_rn(1.0f, __fsub_rn(xhi, xlo));
-    const float vinv = __fdiv_rn(1.0f, __fsub_rn(vhi, vlo));
-    const uint32_t qx = quantise(st[(kX + d) * cap + j], xlo, xinv, xs);
-    const uint32_t qv = quantise(st[(kV + d) * cap + j], vlo, vinv, vs);
+    const uint32_t qx = quantise(st[(kX + d) * cap + j], lo_s[d], inv_s[d], xs);
+    const uint32_t qv = quantise(st[(kV + d) * cap + j], lo_s[3 + d], inv_s[3 + d], vs);
     out[id * 3 + d] = (qx << kVBits) + qv;  // uint32 wrap-around, as numpy
   }
 }

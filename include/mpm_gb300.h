@@ -259,6 +259,29 @@ int mpm_quantize_particles(const float *pstate, int64_t cap, int64_t n, const fl
                            void *stream);
 int mpm_unpack_colors(const int32_t *color, int64_t n, uint8_t *rgb, void *stream);
 
+/* ---- Mesh emitter (engine/voxelizer.py:46-126, engine/mpm_solver.py:1017-1079)
+ * mpm_voxelize: triangles (device float64[ntri * 9], vertex-major xyz) into
+ *   the dense voxel grid `voxels` (device int32[rx * ry * rz], index
+ *   (p * ry + q) * rz + k, zeroed here): per voxel the signed count of
+ *   triangle crossings above it along z, as Voxelizer.voxelize_triangles.
+ *   dx is the voxel size (solver dx / super_sample), padding the voxelizer's.
+ * mpm_voxel_seed_count / mpm_voxel_seed_emit: particles of seed_from_voxels
+ *   (mpm_solver.py:1017-1047).  Count pass: particles per voxel column into
+ *   col_count (int32[rx * ry]); the caller scans them into col_offset
+ *   (int64, exclusive) and sizes x_out (float32[n_out * 3]); the emit pass
+ *   writes positions (rand + (i, j, k)) * voxel_dx + (tx, ty, tz).  Random
+ *   numbers come from a counter-based hash of `seed`, the voxel and the draw
+ *   (deterministic per seed; not Taichi's ti.random stream). */
+int mpm_voxelize(const double *triangles, int64_t ntri, int32_t rx, int32_t ry, int32_t rz, double dx,
+                 int32_t padding, int32_t *voxels, void *stream);
+int mpm_voxel_seed_count(const int32_t *voxels, int32_t rx, int32_t ry, int32_t rz, int32_t sample_density,
+                         int32_t super_sample, int32_t grid_size, int32_t padding, uint64_t seed, int32_t *col_count,
+                         void *stream);
+int mpm_voxel_seed_emit(const int32_t *voxels, int32_t rx, int32_t ry, int32_t rz, int32_t sample_density,
+                        int32_t super_sample, int32_t grid_size, int32_t padding, uint64_t seed, float voxel_dx,
+                        float tx, float ty, float tz, const int64_t *col_offset, int64_t n_out, float *x_out,
+                        void *stream);
+
 /* Pointer to the device status word inside the workspace (uint32). */
 int mpm_status_ptr(const MpmParams *p, void *ws, int64_t cap, uint32_t **status_out);
 

@@ -111,6 +111,10 @@ SIGNATURES = {
     "mpm_particle_ranges": [_v, _i64, _i64, _v, _v, _v],
     "mpm_quantize_particles": [_v, _i64, _i64, _v, _v, _v],
     "mpm_unpack_colors": [_v, _i64, _v, _v],
+    "mpm_voxelize": [_v, _i64, _i32, _i32, _i32, ctypes.c_double, _i32, _v, _v],
+    "mpm_voxel_seed_count": [_v, _i32, _i32, _i32, _i32, _i32, _i32, _i32, ctypes.c_uint64, _v, _v],
+    "mpm_voxel_seed_emit": [_v, _i32, _i32, _i32, _i32, _i32, _i32, _i32, ctypes.c_uint64, _f, _f, _f, _f, _v,
+                            _i64, _v, _v],
     "mpm_g2p_adj": [_P, _v, _i64, _i64, _v, _f, _v, _v, _v, _i32, _v],
     "mpm_grid_adj": [_P, _v, _i64, _v, _v, _f, _v],
     "mpm_p2g_adj": [_P, _v, _i64, _i64, _v, _f, _v, _v, _v, _v, _i32, _v],

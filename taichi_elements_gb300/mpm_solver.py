@@ -151,7 +151,8 @@ class MPMSolver:
         sin_phi = math.sin(friction_angle)
         self.alpha = math.sqrt(2 / 3) * 2 * sin_phi / (3 - sin_phi)
         self.total_substeps = 0
-        self.voxelizer = None
+        self.voxelizer = None  # built on the first add_mesh (engine/mpm_solver.py:284-293)
+        self.use_voxelizer = bool(use_voxelizer)
         self.voxelizer_super_sample = voxelizer_super_sample
         self.writers = []
 
@@ -181,6 +182,8 @@ class MPMSolver:
         self._maxv = torch.zeros(1024, dtype=torch.float32, device=self.device)
         self._gen = torch.Generator(device=self.device)
         self._gen.manual_seed(int(seed))
+        self._seed = int(seed)
+        self._mesh_seed = 0
         self._seed_lo = None  # bounding box (in nodes) of all seeded regions
         self._seed_hi = None
         self._set_window(*self._box_window())
@@ -499,8 +502,30 @@ class MPMSolver:
         self._note_region(*self._finite_bounds(x))
         self._append(x.to(self.device), m, c, v, E=None)
 
-    def add_mesh(self, *args, **kwargs):
-        raise NotImplementedError("add_mesh (voxelizer emitter) is not part of the GB300 engine")
+    def add_mesh(self, triangles, material, color=0xFFFFFF, sample_density=None, velocity=None, translation=None,
+                 emmiter_id=0):
+        """engine/mpm_solver.py:1049-1079: voxelize a triangle mesh (n, 9) on
+        the GPU and seed particles in the voxels inside it
+        (seed_from_voxels, :1017-1047)."""
+        assert self.dim == 3
+        if not self.use_voxelizer:
+            raise RuntimeError("add_mesh needs MPMSolver(use_voxelizer=True)")
+        if sample_density is None:
+            sample_density = 2**self.dim
+        self.set_source_velocity(velocity=velocity)
+        t = [float(translation[i]) if translation else 0.0 for i in range(self.dim)]
+        if self.voxelizer is None:
+            from .voxelizer import Voxelizer
+            self.voxelizer = Voxelizer(res=self.res, dx=self.dx, padding=self.padding,
+                                       super_sample=self.voxelizer_super_sample, device=self.device)
+        self.voxelizer.voxelize(triangles)
+        self._mesh_seed += 1
+        x = self.voxelizer.seed_particles(sample_density, self.grid_size, self.padding, t,
+                                          self._seed * 1000003 + self._mesh_seed)
+        if x.shape[0] == 0:
+            return
+        self._note_region(*self._finite_bounds(x))
+        self._append(x, material, color, self.source_velocity, emitter_id=emmiter_id)
 
     def add_ngon(self, *args, **kwargs):
         raise ValueError("Add Ngon only works for 2D simulations")

@@ -204,3 +204,65 @@ def smoke_scene(seed: int = 7) -> Scene:
     pp = [dict(kind=1, surface=1, point=(0.5, 0.35, 0.5), radius=0.08),
           dict(kind=0, surface=2, point=(0.5, 0.12, 0.5), normal=(0.1, 1.0, 0.0), friction=0.2)]
     return Scene("smoke_24", res, x, np.ascontiguousarray(v), m, 10, postprocess=pp)
+
+
+# ------------------------------------------------------------- meshes ----
+# Closed triangle meshes (n, 9) float32 for the add_mesh emitter; the
+# reference's own mesh tests download theirs, these stand in for them.
+
+def box_mesh(lo, hi) -> np.ndarray:
+    """Axis-aligned box, outward-facing triangles."""
+    lo, hi = np.asarray(lo, np.float64), np.asarray(hi, np.float64)
+    c = np.array([[lo[0] if i & 1 == 0 else hi[0], lo[1] if i & 2 == 0 else hi[1], lo[2] if i & 4 == 0 else hi[2]]
+                  for i in range(8)])
+    quads = [(0, 2, 6, 4), (1, 5, 7, 3), (0, 4, 5, 1), (2, 3, 7, 6), (0, 1, 3, 2), (4, 6, 7, 5)]
+    tris = []
+    for a, b, cc, d in quads:
+        tris += [(a, cc, b), (a, d, cc)]
+    return np.array([np.concatenate([c[i], c[j], c[k]]) for i, j, k in tris], np.float32)
+
+
+def icosphere(center, radius, subdiv=3) -> np.ndarray:
+    """Sphere from a subdivided icosahedron."""
+    t = (1.0 + 5**0.5) / 2
+    v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t), (0, 1, -t), (t, 0, -1),
+         (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    v = [np.array(p, np.float64) / np.linalg.norm(p) for p in v]
+    f = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2), (10, 7, 6),
+         (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10),
+         (8, 6, 7), (9, 8, 1)]
+    for _ in range(subdiv):
+        cache = {}
+
+        def mid(i, j):
+            key = (min(i, j), max(i, j))
+            if key not in cache:
+                m = v[i] + v[j]
+                v.append(m / np.linalg.norm(m))
+                cache[key] = len(v) - 1
+            return cache[key]
+
+        nf = []
+        for a, b, c in f:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            nf += [(a, ab, ca), (b, bc, ab), (c, ca, bc), (ab, bc, ca)]
+        f = nf
+    cen = np.asarray(center, np.float64)
+    return np.array([np.concatenate([cen + radius * v[a], cen + radius * v[b], cen + radius * v[c]]) for a, b, c in f],
+                    np.float32)
+
+
+def torus_mesh(center, R, r, nu=48, nv=24) -> np.ndarray:
+    """Torus around the y axis."""
+    cen = np.asarray(center, np.float64)
+
+    def p(i, j):
+        u, w = 2 * np.pi * i / nu, 2 * np.pi * j / nv
+        return cen + np.array([(R + r * np.cos(w)) * np.cos(u), r * np.sin(w), (R + r * np.cos(w)) * np.sin(u)])
+
+    tris = []
+    for i in range(nu):
+        for j in range(nv):
+            a, b, c, d = p(i, j), p(i + 1, j), p(i + 1, j + 1), p(i, j + 1)
+            tris += [np.concatenate([a, c, b]), np.concatenate([a, d, c])]
+    return np.array(tris, np.float32)

@@ -117,15 +117,24 @@ __global__ __launch_bounds__(kVoxThreads) void k_voxelize(const double *__restri
   }
 }
 
-// difference array -> counts: running sum along z of each column
+// difference array -> counts: running sum along z of each column; one warp
+// per column, lanes over consecutive z (coalesced), a warp scan per 32
 __global__ __launch_bounds__(kVoxThreads) void k_vox_scan(VoxGrid g, int32_t *__restrict__ vox) {
-  const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int64_t col = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (col >= (int64_t)g.rx * g.ry) return;
   int32_t *c = vox + col * g.rz;
-  int32_t run = 0;
-  for (int k = 0; k < g.rz; ++k) {
-    run += c[k];
-    c[k] = run;
+  int32_t carry = 0;
+  for (int k0 = 0; k0 < g.rz; k0 += 32) {
+    const int k = k0 + lane;
+    int32_t v = k < g.rz ? c[k] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int32_t u = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += u;
+    }
+    if (k < g.rz) c[k] = carry + v;
+    carry += __shfl_sync(0xffffffffu, v, 31);
   }
 }
 
@@ -151,42 +160,62 @@ struct SeedParams {
   float tx, ty, tz;
 };
 
+// Draw l of a voxel emits when rand + l < s (float32).  rand lies in
+// [0, 1 - 2^-24], and float32 addition is monotonic, so l >= s never emits
+// and (1 - 2^-24) + l < s always does; only the draw in between is random.
+__device__ __forceinline__ bool emits_draw(const SeedParams &sp, uint64_t vidx, int l) {
+  const float fl = (float)l;
+  if (fl >= sp.s) return false;
+  if (__fadd_rn(0.99999994f, fl) < sp.s) return true;
+  return __fadd_rn(rand01(sp.seed, vidx, 4 * l), fl) < sp.s;
+}
+
 // particles voxel (i, j, k) emits: l in [0, sample_density] with rand + l < s
 __device__ __forceinline__ int voxel_emits(const VoxGrid &g, const SeedParams &sp, int i, int64_t vidx, int32_t count) {
   // mpm_solver.py:1026-1029 tests index i only, for each of the 3 axes
   const bool inside = -sp.grid_size / 2 + sp.padding <= i && i < sp.grid_size / 2 - sp.padding;
   if (!inside || count <= 0) return 0;
   int m = 0;
-  for (int l = 0; l <= sp.sample_density; ++l)
-    if (__fadd_rn(rand01(sp.seed, vidx, 4 * l), (float)l) < sp.s) ++m;
+  for (int l = 0; l <= sp.sample_density && (float)l < sp.s; ++l) m += emits_draw(sp, vidx, l);
   return m;
 }
 
+// one warp per voxel column, lanes over consecutive z
 __global__ __launch_bounds__(kVoxThreads) void k_seed_count(VoxGrid g, SeedParams sp, const int32_t *__restrict__ vox,
                                                            int32_t *__restrict__ col_count) {
-  const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int64_t col = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (col >= (int64_t)g.rx * g.ry) return;
   const int i = (int)(col / g.ry);
   int m = 0;
-  for (int k = 0; k < g.rz; ++k) m += voxel_emits(g, sp, i, col * g.rz + k, vox[col * g.rz + k]);
-  col_count[col] = m;
+  for (int k = lane; k < g.rz; k += 32) m += voxel_emits(g, sp, i, col * g.rz + k, vox[col * g.rz + k]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m += __shfl_xor_sync(0xffffffffu, m, o);
+  if (lane == 0) col_count[col] = m;
 }
 
 __global__ __launch_bounds__(kVoxThreads) void k_seed_emit(VoxGrid g, SeedParams sp, const int32_t *__restrict__ vox,
                                                           const int64_t *__restrict__ col_offset, int64_t n_out,
                                                           float *__restrict__ x_out) {
-  const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int64_t col = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (col >= (int64_t)g.rx * g.ry) return;
   const int i = (int)(col / g.ry), j = (int)(col % g.ry);
-  int64_t o = col_offset[col];
-  for (int k = 0; k < g.rz; ++k) {
+  int64_t base = col_offset[col];
+  for (int k0 = 0; k0 < g.rz; k0 += 32) {
+    const int k = k0 + lane;
     const int64_t vidx = col * g.rz + k;
-    const int32_t cnt = vox[vidx];
-    const bool inside = -sp.grid_size / 2 + sp.padding <= i && i < sp.grid_size / 2 - sp.padding;
-    if (!inside || cnt <= 0) continue;
-    for (int l = 0; l <= sp.sample_density; ++l) {
-      if (!(__fadd_rn(rand01(sp.seed, vidx, 4 * l), (float)l) < sp.s)) continue;
-      if (o >= n_out) return;  // the count pass and this pass agree; never write past the output
+    const int m = k < g.rz ? voxel_emits(g, sp, i, vidx, vox[vidx]) : 0;
+    int incl = m;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += u;
+    }
+    int64_t o = base + incl - m;
+    for (int l = 0; m > 0 && l <= sp.sample_density && (float)l < sp.s; ++l) {
+      if (!emits_draw(sp, vidx, l)) continue;
+      if (o >= n_out) break;  // the count pass and this pass agree; never write past the output
       const float r0 = rand01(sp.seed, vidx, 4 * l + 1), r1 = rand01(sp.seed, vidx, 4 * l + 2),
                   r2 = rand01(sp.seed, vidx, 4 * l + 3);
       // x = (rand3 + (i, j, k)) * (dx / super_sample) + translation, float32
@@ -195,6 +224,7 @@ __global__ __launch_bounds__(kVoxThreads) void k_seed_emit(VoxGrid g, SeedParams
       x_out[o * 3 + 2] = __fadd_rn(__fmul_rn(__fadd_rn(r2, (float)k), sp.vdx), sp.tz);
       ++o;
     }
+    base += __shfl_sync(0xffffffffu, incl, 31);
   }
 }
 
@@ -221,7 +251,7 @@ int mpm_voxelize(const double *triangles, int64_t ntri, int32_t rx, int32_t ry, 
                                                                                             voxels);
   }
   const int64_t cols = (int64_t)rx * ry;
-  k_vox_scan<<<(unsigned)((cols + kVoxThreads - 1) / kVoxThreads), kVoxThreads, 0, s>>>(g, voxels);
+  k_vox_scan<<<(unsigned)((cols * 32 + kVoxThreads - 1) / kVoxThreads), kVoxThreads, 0, s>>>(g, voxels);
   return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_E_CUDA;
 }
 
@@ -234,7 +264,7 @@ int mpm_voxel_seed_count(const int32_t *voxels, int32_t rx, int32_t ry, int32_t 
   const float ss3 = (float)super_sample * (float)super_sample * (float)super_sample;
   SeedParams sp{sample_density, (float)sample_density / ss3, grid_size, padding, seed, 0.f, 0.f, 0.f, 0.f};
   const int64_t cols = (int64_t)rx * ry;
-  k_seed_count<<<(unsigned)((cols + kVoxThreads - 1) / kVoxThreads), kVoxThreads, 0, (cudaStream_t)stream>>>(
+  k_seed_count<<<(unsigned)((cols * 32 + kVoxThreads - 1) / kVoxThreads), kVoxThreads, 0, (cudaStream_t)stream>>>(
       g, sp, voxels, col_count);
   return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_E_CUDA;
 }
@@ -250,7 +280,7 @@ int mpm_voxel_seed_emit(const int32_t *voxels, int32_t rx, int32_t ry, int32_t r
   const float ss3 = (float)super_sample * (float)super_sample * (float)super_sample;
   SeedParams sp{sample_density, (float)sample_density / ss3, grid_size, padding, seed, voxel_dx, tx, ty, tz};
   const int64_t cols = (int64_t)rx * ry;
-  k_seed_emit<<<(unsigned)((cols + kVoxThreads - 1) / kVoxThreads), kVoxThreads, 0, (cudaStream_t)stream>>>(
+  k_seed_emit<<<(unsigned)((cols * 32 + kVoxThreads - 1) / kVoxThreads), kVoxThreads, 0, (cudaStream_t)stream>>>(
       g, sp, voxels, col_offset, n_out, x_out);
   return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_E_CUDA;
 }

@@ -149,6 +149,20 @@ int mpm_g2p(const MpmParams *p, void *ws, int64_t cap, int64_t n, float *nxt, fl
 int mpm_substep(const MpmParams *p, void *ws, int64_t cap, int64_t n, const float *cur, float *nxt,
                 float dt, float *maxv_out, void *stream);
 
+/* One substep of the fused G2P2G mode (MPMSolver(use_g2p2g=True),
+ * engine/mpm_solver.py:363-485 and :773-787): G2P from the grid velocities of
+ * the previous substep, advection, the constitutive update and P2G at the new
+ * positions in one kernel, then the binning of the new positions and the grid
+ * update with dt.  Particles with id >= first_new skip the gather (they keep
+ * their v, C = 0), as particles added since the last substep do in the
+ * reference (last_time_final_particles).  C is not stored in this mode.
+ * The workspace must hold the binning of `cur`: finalized lists when
+ * finalize_first == 0 (the state after a previous call), or the counts of
+ * every particle when finalize_first != 0.  After the call it holds the
+ * finalized lists of `nxt` and the grid velocities the next call gathers. */
+int mpm_g2p2g_substep(const MpmParams *p, void *ws, int64_t cap, int64_t n, const float *cur, float *nxt,
+                      float dt, int64_t first_new, int32_t finalize_first, float *maxv_out, void *stream);
+
 /* Batched form: bins particles [begin, end) of a multi-scene state.  `p` is
  * the batch header (window, chunk, slot layout, n_scenes) and `scenes` a
  * device array of n_scenes per-scene MpmParams rows (see MpmParams).  No

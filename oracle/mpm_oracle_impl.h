@@ -254,9 +254,12 @@ static void FN(sand_projection)(REAL sig[3], REAL *Jp, const FN(Consts) * k, REA
 
 /* One particle's P2G update (engine/mpm_solver.py:495-575): updates F and Jp
  * in place and returns the scatter inputs (mass, momentum m*v, affine). */
+/* fused != 0: the constitutive update of the G2P2G substep (:410-476):
+ * no water F reset (:508-511), h = exp(10 (1 - Jp)) for every material,
+ * water keeps Jp, mass = p_mass for every material. */
 static void FN(p2g_particle)(const FN(Consts) * k, REAL dt, int mat, REAL Ep,
                              REAL *F9, REAL *Jp, const REAL *C9, REAL *mass_out,
-                             REAL affine[3][3]) {
+                             REAL affine[3][3], int fused) {
   REAL mu0 = k->mu0, la0 = k->la0;
   if (Ep > (REAL)0) { /* per-particle Young's modulus (extension) */
     mu0 = Ep / ((REAL)2 * ((REAL)1 + k->nu));
@@ -268,7 +271,7 @@ static void FN(p2g_particle)(const FN(Consts) * k, REAL dt, int mat, REAL Ep,
       F[i][j] = F9[3 * i + j];
       C[i][j] = C9[3 * i + j];
     }
-  if (mat == 0) { /* :508-511 */
+  if (!fused && mat == 0) { /* :508-511 */
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) F[i][j] = (REAL)(i == j);
     F[0][0] = *Jp;
@@ -277,7 +280,7 @@ static void FN(p2g_particle)(const FN(Consts) * k, REAL dt, int mat, REAL Ep,
     for (int j = 0; j < 3; ++j) G[i][j] = (REAL)(i == j) + dt * C[i][j];
   FN(matmul3)(G, F, Fn); /* :513 */
   REAL h = 1;
-  if (mat != 0) h = EXP((REAL)10 * ((REAL)1 - *Jp)); /* :516-518 */
+  if (fused || mat != 0) h = EXP((REAL)10 * ((REAL)1 - *Jp)); /* :516-518, :427-429 */
   if (mat == 1) h = (REAL)0.3;                         /* :519-521 */
   REAL mu = mu0 * h, la = la0 * h;
   if (mat == 0) mu = 0;
@@ -307,7 +310,7 @@ static void FN(p2g_particle)(const FN(Consts) * k, REAL dt, int mat, REAL Ep,
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) Fn[i][j] = (REAL)(i == j);
     Fn[0][0] = J;
-    *Jp = J;
+    if (!fused) *Jp = J;
   } else if (mat == 2) { /* :543-545 */
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j)
@@ -347,7 +350,7 @@ static void FN(p2g_particle)(const FN(Consts) * k, REAL dt, int mat, REAL Ep,
     for (int j = 0; j < 3; ++j) F9[3 * i + j] = Fn[i][j]; /* :567 */
   REAL sc = -dt * k->stress_scale_k;                     /* :569 */
   REAL mass = k->p_mass;
-  if (mat == 0) mass *= k->water_density; /* :571-573 */
+  if (!fused && mat == 0) mass *= k->water_density; /* :571-573 */
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) affine[i][j] = sc * stress[i][j] + mass * C[i][j]; /* :574 */
   *mass_out = mass;
@@ -519,7 +522,7 @@ int FN(oracle_p2g)(const double *pd, int64_t n, const REAL *x, const REAL *v, co
 #pragma omp parallel for num_threads(nthreads) schedule(static) reduction(+ : bad) if (atomic)
   for (int64_t p = 0; p < n; ++p) {
     REAL affine[3][3], mass;
-    FN(p2g_particle)(&k, dt, mat[p], E_p ? E_p[p] : (REAL)0, F + 9 * p, Jp + p, C + 9 * p, &mass, affine);
+    FN(p2g_particle)(&k, dt, mat[p], E_p ? E_p[p] : (REAL)0, F + 9 * p, Jp + p, C + 9 * p, &mass, affine, 0);
     bad += FN(scatter_particle)(&w, x + 3 * p, v + 3 * p, &k, mass, affine, gm, gmv, atomic);
   }
   return bad;
@@ -557,6 +560,59 @@ int FN(oracle_g2p)(const double *pd, int64_t n, REAL *x, REAL *v, REAL *C, const
 #pragma omp parallel for num_threads(nthreads) schedule(static) reduction(+ : bad)
   for (int64_t p = 0; p < n; ++p)
     bad += FN(g2p_particle)(&w, &k, dt, mat[p], x + 3 * p, v + 3 * p, C + 9 * p, gv);
+  return bad;
+}
+
+/* One G2P2G substep (engine/mpm_solver.py:363-485, step :773-787) on dense
+ * window grids: for every particle, G2P from gv_in (node velocities of the
+ * previous substep, AoS) at x -- particles p >= first_new keep v with C = 0
+ * (:401-404) -- advection unless stationary (:406-408), the fused
+ * constitutive update, and P2G at the new x into gm / gmv (zeroed by the
+ * caller); then the grid update of every window node (normalisation, gravity,
+ * post-process list), leaving the new node velocities in gmv.  Returns the
+ * number of particles whose stencil left the window. */
+int FN(oracle_g2p2g)(const double *pd, const int32_t *res, int padding, int unbounded, int grid_size, int ncoll,
+                     const double *coll, int64_t n, int64_t first_new, REAL *x, REAL *v, REAL *F, REAL *Jp,
+                     const int32_t *mat, const REAL *E_p, REAL dt, const int32_t *lo, const int32_t *W,
+                     const REAL *gv_in, REAL *gm, REAL *gmv) {
+  FN(Consts) k;
+  FN(make_consts)(pd, &k);
+  FN(Window) w;
+  for (int d = 0; d < 3; ++d) {
+    w.lo[d] = lo[d];
+    w.W[d] = W[d];
+  }
+  int bad = 0;
+  for (int64_t p = 0; p < n; ++p) {
+    REAL nv[3] = {v[3 * p], v[3 * p + 1], v[3 * p + 2]};
+    REAL C9[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    if (p < first_new) {
+      REAL xs[3] = {x[3 * p], x[3 * p + 1], x[3 * p + 2]};
+      /* the gather of g2p_particle, applied to scratch copies (mat 0 so that
+       * it writes v and C; x is advected below) */
+      REAL xg[3] = {xs[0], xs[1], xs[2]};
+      if (FN(g2p_particle)(&w, &k, (REAL)0, 0, xg, nv, C9, gv_in)) {
+        bad += 1;
+        continue;
+      }
+    }
+    if (mat[p] != 4) {
+      for (int d = 0; d < 3; ++d) {
+        v[3 * p + d] = nv[d];
+        x[3 * p + d] += dt * v[3 * p + d];
+      }
+    }
+    REAL affine[3][3], mass;
+    FN(p2g_particle)(&k, dt, mat[p], E_p ? E_p[p] : (REAL)0, F + 9 * p, Jp + p, C9, &mass, affine, 1);
+    bad += FN(scatter_particle)(&w, x + 3 * p, v + 3 * p, &k, mass, affine, gm, gmv, 0);
+  }
+  for (int i = 0; i < W[0]; ++i)
+    for (int j = 0; j < W[1]; ++j)
+      for (int kk = 0; kk < W[2]; ++kk) {
+        int64_t nn = ((int64_t)i * W[1] + j) * W[2] + kk;
+        FN(grid_node)(lo[0] + i, lo[1] + j, lo[2] + kk, gm[nn], gmv + 3 * nn, dt, &k, res, padding, unbounded,
+                      grid_size, ncoll, coll);
+      }
   return bad;
 }
 
@@ -627,7 +683,7 @@ int FN(oracle_substeps)(const double *pd, const int32_t *res, int padding, int u
       for (int64_t q = st; q < bcount[b]; ++q) {
         int64_t p = order[q];
         REAL affine[3][3], mass;
-        FN(p2g_particle)(&k, dt, mat[p], E_p ? E_p[p] : (REAL)0, F + 9 * p, Jp + p, C + 9 * p, &mass, affine);
+        FN(p2g_particle)(&k, dt, mat[p], E_p ? E_p[p] : (REAL)0, F + 9 * p, Jp + p, C + 9 * p, &mass, affine, 0);
         FN(scatter_particle)(&w, x + 3 * p, v + 3 * p, &k, mass, affine, gm, gmv, nthreads > 1);
       }
     }

@@ -62,6 +62,9 @@ def lib() -> ctypes.CDLL:
                                                             vp, vp, real, i32, vp, vp, vp, vp, vp, vp, vp, vp, i32,
                                                             vp]
             getattr(L, "oracle_substeps" + sfx).restype = i32
+            getattr(L, "oracle_g2p2g" + sfx).argtypes = [vp, vp, i32, i32, i32, i32, vp, i64, i64, vp, vp, vp, vp,
+                                                         vp, vp, real, vp, vp, vp, vp, vp]
+            getattr(L, "oracle_g2p2g" + sfx).restype = i32
         _lib = L
     return _lib
 
@@ -323,6 +326,35 @@ class Runner:
         if bad:
             raise ValueError(f"{bad} particles left the oracle window")
         return maxv
+
+
+class G2P2GRunner:
+    """The fused G2P2G mode (engine/mpm_solver.py:363-485, :773-787): the
+    grid velocities persist between substeps; particles added since the last
+    substep (index >= last_final) skip the gather.  C is not carried."""
+
+    def __init__(self, cfg: Config, P: Particles, win: Window):
+        self.cfg, self.P, self.win = cfg, P, win
+        self.gv = np.zeros(win.nnodes * 3, P.x.dtype)
+        self.last_final = 0
+        self.res = np.asarray(cfg.res, dtype=np.int32)
+        self.coll = cfg.coll()
+
+    def step(self, dt: float):
+        P = self.P
+        dt_ = P.x.dtype
+        sfx = "_d" if dt_ == np.float64 else "_f"
+        gm = np.zeros(self.win.nnodes, dt_)
+        gmv = np.zeros(self.win.nnodes * 3, dt_)
+        bad = getattr(lib(), "oracle_g2p2g" + sfx)(
+            _p(self.cfg.pd()), _p(self.res), self.cfg.padding, int(self.cfg.unbounded), self.cfg.grid_size,
+            len(self.cfg.postprocess), _p(self.coll), P.n, self.last_final, _p(P.x), _p(P.v), _p(P.F), _p(P.Jp),
+            _p(P.material), _p(P.E), dt_.type(dt), _p(self.win.lo), _p(self.win.W), _p(self.gv), _p(gm), _p(gmv))
+        if bad:
+            raise ValueError(f"{bad} particles left the oracle window")
+        self.gv = gmv
+        self.last_final = P.n
+        return gm.reshape(tuple(self.win.W)), gmv.reshape(tuple(self.win.W) + (3,))
 
 
 # ------------------------------------------------- numpy restatement ---

@@ -180,7 +180,11 @@ struct P2GOut {
 };
 
 // Per-particle P2G update, engine/mpm_solver.py:506-574 with sand_projection
-// :321-342.  F and Jp are updated in place.
+// :321-342.  F and Jp are updated in place.  FUSED selects the variant of the
+// fused G2P2G substep (:419-476): no water F reset before the update
+// (:508-511), hardening h = exp(10 (1 - Jp)) for every material, water keeps
+// its Jp (:537-542 sets only F) and the mass is p_mass for every material.
+template <bool FUSED = false>
 __device__ __forceinline__ P2GOut constitutive(const MpmParams &P, float dt, int mat, float Ep,
                                                float (&F)[3][3], float &Jp, const float (&C)[3][3]) {
   float mu0 = P.mu0, la0 = P.la0;
@@ -188,7 +192,7 @@ __device__ __forceinline__ P2GOut constitutive(const MpmParams &P, float dt, int
     mu0 = Ep / (2.0f * (1.0f + P.nu));
     la0 = Ep * P.nu / ((1.0f + P.nu) * (1.0f - 2.0f * P.nu));
   }
-  if (mat == 0) {  // :508-511
+  if (!FUSED && mat == 0) {  // :508-511
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -207,7 +211,7 @@ __device__ __forceinline__ P2GOut constitutive(const MpmParams &P, float dt, int
       Fn[i][j] = acc;
     }
   float h = 1.0f;
-  if (mat != 0) h = expf(10.0f * (1.0f - Jp));  // :516-518
+  if (FUSED || mat != 0) h = expf(10.0f * (1.0f - Jp));  // :516-518 (:427-429)
   if (mat == 1) h = 0.3f;                       // :519-521
   float mu = mu0 * h;
   const float la = la0 * h;
@@ -228,7 +232,7 @@ __device__ __forceinline__ P2GOut constitutive(const MpmParams &P, float dt, int
         stress[i][j] = (i == j) ? la * J * (J - 1.0f) : 0.0f;
       }
     Fn[0][0] = J;
-    Jp = J;
+    if (!FUSED) Jp = J;
   } else {
     if (mat == 1 || mat == 4 || mat == 2) {
       // Elastic and stationary particles never clamp sigma (:527-536), and a
@@ -365,7 +369,7 @@ done:
   P2GOut o;
   const float sc = -dt * P.stress_k;  // :569
   o.mass = P.p_mass;
-  if (mat == 0) o.mass *= P.water_density;  // :571-573
+  if (!FUSED && mat == 0) o.mass *= P.water_density;  // :571-573
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll

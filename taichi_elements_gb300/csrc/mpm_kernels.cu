@@ -645,6 +645,229 @@ __global__ __launch_bounds__(kG2PThreads, 8) void k_g2p(const MpmParams P, const
   }
 }
 
+// -------------------------------------------------------------- G2P2G ----
+//
+// The fused substep of use_g2p2g=True (engine/mpm_solver.py:363-485): per
+// particle, G2P from the grid velocities of the previous substep at x
+// (particles added since then keep their v with C = 0, :401-404), advection,
+// the constitutive update with the gathered C (C is not stored), and P2G at
+// the advected position into the momentum grid of this substep.  Work items
+// are the blocks of the particles' positions before advection, so the
+// scatter reaches the nodes [-1, 6] of the block per axis: an 8^3 float4 tile
+// per warp, flushed like P2G.  A particle that moved more than one cell
+// scatters straight to the grid with global atomics.  The new positions are
+// binned for the next substep, as in G2P.
+
+constexpr int kFusedTileW = 8;
+constexpr int kFusedTileN = kFusedTileW * kFusedTileW * kFusedTileW;
+
+__global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_g2p2g(const MpmParams P, const Ws w,
+                                                                         const float *__restrict__ cur,
+                                                                         float *__restrict__ nxt, int64_t cap,
+                                                                         float dt, int64_t first_new,
+                                                                         float *maxv_out) {
+  __shared__ float4 vt[kTileN];
+  __shared__ float4 tiles[kP2GWarps][kFusedTileN];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float4 *tile = tiles[warp];
+  const int nitems = (int)min((int64_t)w.counters[2], w.items_cap);
+  const float s4 = 4.0f * P.inv_dx;
+  uint32_t bad = 0;
+  float vmax = 0.0f;
+  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
+    const int2 item = w.items[it];
+    const int k = item.x, start = item.y;
+    const int end = (int)min((int64_t)min(start + P.chunk, w.pb_start[k] + w.pb_count[k]), cap);
+    int bx, by, bz;
+    block_coords(P, w.pblocks[k], bx, by, bz);
+    for (int t = threadIdx.x; t < kTileN; t += blockDim.x) {
+      const int tx = t / 36, ty = (t / 6) % 6, tz = t % 6;
+      const int gx = bx * 4 + tx, gy = by * 4 + ty, gz = bz * 4 + tz;
+      float4 g = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (gx < P.win_nb[0] * 4 && gy < P.win_nb[1] * 4 && gz < P.win_nb[2] * 4)
+        g = w.grid_vel[node_addr(P, gx, gy, gz)];
+      vt[t] = g;
+    }
+    for (int t = lane; t < kFusedTileN; t += 32) tile[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncthreads();
+    for (int j0 = start + warp * 32; j0 < end; j0 += kP2GThreads) {
+      const int j = j0 + lane;
+      bool active = j < end;
+      int64_t i = active ? w.pid[j] : 0;
+      if (active && (i < 0 || i >= cap)) {
+        bad |= MPM_STATUS_TABLE_OVERFLOW;
+        active = false;
+      }
+      int cell = -1 - lane;  // unique per inactive lane
+      bool direct = false;   // moved more than a cell: scatter with global atomics
+      float mass = 0.f, q[3] = {0.f, 0.f, 0.f}, adx[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+      float wt[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+      int tx0 = 0, ty0 = 0, tz0 = 0, gb[3] = {0, 0, 0};
+      if (active) {
+        const float *src = cur + i;
+        float *dst = nxt + j;
+        float x[3], v[3], F[3][3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          x[d] = src[(kX + d) * cap];
+          v[d] = src[(kV + d) * cap];
+        }
+#pragma unroll
+        for (int a = 0; a < 9; ++a) F[a / 3][a % 3] = src[(kF + a) * cap];
+        float Jp = src[kJp * cap];
+        const int matword = __float_as_int(src[kMat * cap]);
+        const int mat = matword & 0xFF;
+        const float idf = src[kId * cap];
+        const float Ep = P.has_Ep ? src[kEp * cap] : 0.0f;
+        // ---- G2P at x (:373-404) ----
+        const Base b = particle_base(P, x[0], x[1], x[2], bad);
+        const int lx = b.b[0] - bx * 4, ly = b.b[1] - by * 4, lz = b.b[2] - bz * 4;
+        float C[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+        float nv[3] = {v[0], v[1], v[2]};
+        if ((unsigned)lx > 3u || (unsigned)ly > 3u || (unsigned)lz > 3u) {
+          bad |= MPM_STATUS_TABLE_OVERFLOW;
+          active = false;
+        } else if ((int64_t)__float_as_int(idf) < first_new) {
+          float gw[3][3];
+          bspline_weights(b.fx, gw);
+          nv[0] = nv[1] = nv[2] = 0.0f;
+          const int base_node = (lx * kTileW + ly) * kTileW + lz;
+#pragma unroll
+          for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int bb = 0; bb < 3; ++bb)
+#pragma unroll
+              for (int c = 0; c < 3; ++c) {
+                const float4 g = vt[base_node + (a * kTileW + bb) * kTileW + c];
+                const float wgt = gw[a][0] * gw[bb][1] * gw[c][2];
+                const float dp[3] = {(float)a - b.fx[0], (float)bb - b.fx[1], (float)c - b.fx[2]};
+                const float gv[3] = {g.x, g.y, g.z};
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                  nv[r] += wgt * gv[r];
+#pragma unroll
+                  for (int cc = 0; cc < 3; ++cc) C[r][cc] += s4 * wgt * gv[r] * dp[cc];
+                }
+              }
+        }
+        if (active) {
+          if (mat != 4) {  // :406-408
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+              v[d] = nv[d];
+              x[d] = x[d] + dt * v[d];
+            }
+          }
+          // ---- constitutive update and P2G at the new x (:410-485) ----
+          const P2GOut o = constitutive<true>(P, dt, mat, Ep, F, Jp, C);
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            dst[(kX + d) * cap] = x[d];
+            dst[(kV + d) * cap] = v[d];
+          }
+#pragma unroll
+          for (int a = 0; a < 9; ++a) dst[(kF + a) * cap] = F[a / 3][a % 3];
+          dst[kJp * cap] = Jp;
+          dst[kMat * cap] = __int_as_float(matword);
+          dst[kId * cap] = idf;
+          if (P.has_Ep) dst[kEp * cap] = Ep;
+          vmax = fmaxf(vmax, fmaxf(fabsf(v[0]), fmaxf(fabsf(v[1]), fabsf(v[2]))));
+          const Base b2 = particle_base(P, x[0], x[1], x[2], bad);
+          bspline_weights(b2.fx, wt);
+          mass = o.mass;
+#pragma unroll
+          for (int d = 0; d < 3; ++d)
+            q[d] = o.mass * v[d] -
+                   P.dx * (o.affine[d][0] * b2.fx[0] + o.affine[d][1] * b2.fx[1] + o.affine[d][2] * b2.fx[2]);
+#pragma unroll
+          for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) adx[r][c] = o.affine[r][c] * P.dx;
+          tx0 = b2.b[0] - bx * 4 + 1;
+          ty0 = b2.b[1] - by * 4 + 1;
+          tz0 = b2.b[2] - bz * 4 + 1;
+#pragma unroll
+          for (int d = 0; d < 3; ++d) gb[d] = b2.b[d];
+          if ((unsigned)tx0 > 5u || (unsigned)ty0 > 5u || (unsigned)tz0 > 5u) {
+            direct = true;
+          } else {
+            cell = (tx0 * kFusedTileW + ty0) * kFusedTileW + tz0;
+          }
+          bin_one<false>(P, nullptr, w, j, x[0], x[1], x[2], matword, bad);  // next substep's build_pid
+        }
+      }
+      if (active && direct) {  // rare: straight to the grid
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int bb = 0; bb < 3; ++bb)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              const int gx = gb[0] + a, gy = gb[1] + bb, gz = gb[2] + c;
+              if (gx < 0 || gy < 0 || gz < 0 || gx >= P.win_nb[0] * 4 || gy >= P.win_nb[1] * 4 ||
+                  gz >= P.win_nb[2] * 4)
+                continue;
+              const float wgt = wt[a][0] * wt[bb][1] * wt[c][2];
+              float4 g;
+              g.x = wgt * mass;
+              g.y = wgt * (q[0] + adx[0][0] * (float)a + adx[0][1] * (float)bb + adx[0][2] * (float)c);
+              g.z = wgt * (q[1] + adx[1][0] * (float)a + adx[1][1] * (float)bb + adx[1][2] * (float)c);
+              g.w = wgt * (q[2] + adx[2][0] * (float)a + adx[2][1] * (float)bb + adx[2][2] * (float)c);
+              atomicAdd(&w.grid_mom[node_addr(P, gx, gy, gz)], g);
+            }
+      }
+      const bool tiled = active && !direct;
+      const unsigned peers = __match_any_sync(0xffffffffu, cell);
+      const int round_of_lane = __popc(peers & ((1u << lane) - 1u));
+      const int base_node = (tiled ? (tx0 * kFusedTileW + ty0) * kFusedTileW + tz0 : 0);
+      for (int round = 0;; ++round) {
+        const bool mine = tiled && round_of_lane == round;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int bb = 0; bb < 3; ++bb) {
+            const float wab = tiled ? wt[a][0] * wt[bb][1] : 0.0f;
+            float pab[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) pab[d] = q[d] + adx[d][0] * (float)a + adx[d][1] * (float)bb;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              const float wgt = wab * wt[c][2];
+              float4 *nd = tile + base_node + (a * kFusedTileW + bb) * kFusedTileW + c;
+              float4 g = *nd;
+              g.x = fmaf(wgt, mass, g.x);
+              g.y = fmaf(wgt, fmaf(adx[0][2], (float)c, pab[0]), g.y);
+              g.z = fmaf(wgt, fmaf(adx[1][2], (float)c, pab[1]), g.z);
+              g.w = fmaf(wgt, fmaf(adx[2][2], (float)c, pab[2]), g.w);
+              if (mine) *nd = g;
+              __syncwarp();
+            }
+          }
+        if (!__any_sync(0xffffffffu, tiled && round_of_lane > round)) break;
+      }
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < kFusedTileN; t += blockDim.x) {
+      float4 g = tiles[0][t];
+#pragma unroll
+      for (int wq = 1; wq < kP2GWarps; ++wq) g = f4add(g, tiles[wq][t]);
+      if (g.x != 0.0f) {
+        const int tx = t / 64, ty = (t / 8) % 8, tz = t % 8;
+        const int gx = bx * 4 - 1 + tx, gy = by * 4 - 1 + ty, gz = bz * 4 - 1 + tz;
+        if (gx >= 0 && gy >= 0 && gz >= 0 && gx < P.win_nb[0] * 4 && gy < P.win_nb[1] * 4 && gz < P.win_nb[2] * 4)
+          atomicAdd(&w.grid_mom[node_addr(P, gx, gy, gz)], g);
+      }
+    }
+    __syncthreads();
+  }
+  set_status(w, bad);
+  if (maxv_out) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+    if ((threadIdx.x & 31) == 0 && vmax > 0.0f) atomicMax((int *)maxv_out, __float_as_int(vmax));
+  }
+}
+
 __global__ void k_gather_rows(const float *__restrict__ ps, int64_t cap, int64_t n, int row0, int ncols,
                               float *__restrict__ out) {
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -658,7 +881,7 @@ __global__ void k_gather_rows(const float *__restrict__ ps, int64_t cap, int64_t
 
 struct DevInfo {
   int sms = 0;
-  int p2g_ctas = 0, p2g_ep_ctas = 0, g2p_ctas = 0;
+  int p2g_ctas = 0, p2g_ep_ctas = 0, g2p_ctas = 0, g2p2g_ctas = 0;
   int p2g_b_ctas = 0, p2g_ep_b_ctas = 0, g2p_b_ctas = 0;
 };
 
@@ -680,6 +903,9 @@ static const DevInfo *dev_info() {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a2, k_p2g<false, true>, kP2GThreads, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_p2g<true, true>, kP2GThreads, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c2, k_g2p<true>, kG2PThreads, 0);
+    int f = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, k_g2p2g, kP2GThreads, 0);
+    d.g2p2g_ctas = sms * (f > 0 ? f : 1);
     d.p2g_ctas = sms * (a > 0 ? a : 1);
     d.p2g_ep_ctas = sms * (b > 0 ? b : 1);
     d.g2p_ctas = sms * (c > 0 ? c : 1);
@@ -835,6 +1061,27 @@ int mpm_g2p_bin_into(const MpmParams *p, void *ws, void *ws_bins, int64_t cap, i
   w.cellkey = wb.cellkey;
   k_g2p<false><<<di->g2p_ctas, kG2PThreads, 0, (cudaStream_t)stream>>>(*p, nullptr, w, nxt, cap, dt, maxv_out);
   return last_error();
+}
+
+int mpm_g2p2g_substep(const MpmParams *p, void *ws, int64_t cap, int64_t n, const float *cur, float *nxt,
+                      float dt, int64_t first_new, int32_t finalize_first, float *maxv_out, void *stream) {
+  if (!params_ok(p) || p->n_scenes > 0 || !ws || !cur || !nxt || n < 0 || n > cap || first_new < 0)
+    return MPM_E_INVALID;
+  const DevInfo *di = dev_info();
+  if (!di) return MPM_E_CUDA;
+  int rc = MPM_OK;
+  if (finalize_first) {
+    rc = mpm_bin_finalize(p, ws, cap, n, stream);
+    if (rc) return rc;
+  }
+  Ws w;
+  ws_layout(*p, cap, (char *)ws, &w);
+  k_g2p2g<<<di->g2p2g_ctas, kP2GThreads, 0, (cudaStream_t)stream>>>(*p, w, cur, nxt, cap, dt, first_new, maxv_out);
+  rc = last_error();
+  if (rc) return rc;
+  rc = mpm_bin_finalize(p, ws, cap, n, stream);
+  if (rc) return rc;
+  return mpm_grid_update(p, ws, cap, dt, stream);
 }
 
 int mpm_substep(const MpmParams *p, void *ws, int64_t cap, int64_t n, const float *cur, float *nxt, float dt,

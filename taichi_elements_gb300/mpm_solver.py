@@ -100,8 +100,6 @@ class MPMSolver:
             raise NotImplementedError("the GB300 engine implements the 3-D solver only")
         if quant:
             raise NotImplementedError("quantised particle storage (quant=True) is not implemented")
-        if use_g2p2g:
-            raise NotImplementedError("the fused G2P2G substep (use_g2p2g=True) is not implemented")
         if not support_plasticity:
             raise NotImplementedError("support_plasticity=False is not implemented")
         if use_adaptive_dt:
@@ -179,6 +177,13 @@ class MPMSolver:
         self._params_version = 0
         self._graphs = {}
         self._graph_seen = set()
+        # fused G2P2G mode (engine/mpm_solver.py:363-485): particles covered by
+        # the finalized binning of the current state, the reference's
+        # last_time_final_particles, and whether the grid velocities of the
+        # previous substep are valid
+        self._g2p2g_listed = 0
+        self._last_final = 0
+        self._g2p2g_grid_valid = False
         self._maxv = torch.zeros(1024, dtype=torch.float32, device=self.device)
         self._gen = torch.Generator(device=self.device)
         self._gen.manual_seed(int(seed))
@@ -337,6 +342,8 @@ class MPMSolver:
         off = sp.value - _ptr(self._ws)
         self._status = self._ws[off:off + 4].view(torch.int32)
         self._binned = 0
+        self._g2p2g_listed = 0
+        self._g2p2g_grid_valid = False  # a new workspace has no grid of the previous substep
         self._graphs.clear()
 
     def _ensure_capacity(self, extra: int):
@@ -366,6 +373,12 @@ class MPMSolver:
     def _rebin(self):
         """Bin particles that are not binned yet (all after a workspace reset)."""
         self._ensure_workspace()
+        if self.use_g2p2g and self._g2p2g_listed:
+            if self._g2p2g_listed == self.n_particles:
+                return  # the finalized binning of the last substep covers every particle
+            # particles were added since: the counts were consumed, count all again
+            self._binned = 0
+            self._g2p2g_listed = 0
         if self._binned < self.n_particles:
             p = self.params
             _lib.check(
@@ -570,6 +583,18 @@ class MPMSolver:
         cur = self._state[self._cur]
         nxt = self._state[1 - self._cur]
         mv = _ptr(self._maxv) + 4 * maxv_slot if maxv_slot >= 0 else None
+        if self.use_g2p2g:
+            first_new = self._last_final if self._g2p2g_grid_valid else 0
+            _lib.check(
+                self._lib.mpm_g2p2g_substep(ctypes.byref(p), _ptr(self._ws), self._cap, self.n_particles, _ptr(cur),
+                                            _ptr(nxt), float(dt), first_new, 0 if self._g2p2g_listed else 1, mv,
+                                            self.stream), "mpm_g2p2g_substep")
+            self._cur = 1 - self._cur
+            self._g2p2g_listed = self.n_particles
+            self._binned = 0
+            self._last_final = self.n_particles
+            self._g2p2g_grid_valid = True
+            return
         _lib.check(
             self._lib.mpm_substep(ctypes.byref(p), _ptr(self._ws), self._cap, self.n_particles, _ptr(cur), _ptr(nxt),
                                   float(dt), mv, self.stream), "mpm_substep")
@@ -611,6 +636,8 @@ class MPMSolver:
         if count > self._maxv.numel():
             self._maxv = torch.zeros(count, dtype=torch.float32, device=self.device)
         key = (count, float(dt), self._cur, self.n_particles, self._params_version, _ptr(self._ws))
+        if self.use_g2p2g:  # the first substep's launch depends on the mode's state
+            key += (bool(self._g2p2g_listed), self._last_final if self._g2p2g_grid_valid else 0)
         if not self.use_cuda_graph:
             self._maxv[:count].zero_()
             for s in range(count):

@@ -1,0 +1,107 @@
+"""The fused G2P2G mode (MPMSolver(use_g2p2g=True); engine/mpm_solver.py
+:363-485 and the step loop :773-787) against the C oracle's restatement of
+it (oracle_g2p2g, float64 and float32).
+
+Tolerances as for the plain substep: after k substeps, grid velocities on the
+grid-active nodes within rel L-inf 1e-5 and particle x / F / Jp within 1e-6
+(v 1e-5) of float64, or never worse than 4x the float32 oracle's own error;
+100-substep trajectories within rel L2 1e-3 of float64 positions."""
+import numpy as np
+import pytest
+
+from helpers import gpu_grid, oracle_config, rel_inf, window_lookup
+from oracle import oracle as O
+from taichi_elements_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+TOL = {'grid_v': 1e-5, 'x': 1e-6, 'v': 1e-5, 'F': 1e-6, 'Jp': 1e-6}
+
+
+def gpu_particles(s):
+    st = s.full_state()
+    return {k: st[k].cpu().numpy().astype(np.float64) for k in ('x', 'v', 'F', 'Jp')}
+
+
+def errors(s, R64, R32, win):
+    g = gpu_particles(s)
+    coords, vel = gpu_grid(s.views(), 'grid_vel')
+    gv64 = R64.gv.reshape(tuple(win.W) + (3,))
+    gv32 = R32.gv.reshape(tuple(win.W) + (3,))
+    ref_v = window_lookup(win, coords, gv64)
+    vscale = max(np.abs(R64.P.v).max(), 1e-3)
+    fs = max(1.0, np.abs(R64.P.F).max())
+    js = max(1.0, np.abs(R64.P.Jp).max())
+    return {
+        'grid_v': (rel_inf(vel[:, :3], ref_v), rel_inf(window_lookup(win, coords, gv32), ref_v)),
+        'x': (rel_inf(g['x'], R64.P.x, 1.0), rel_inf(R32.P.x, R64.P.x, 1.0)),
+        'v': (rel_inf(g['v'], R64.P.v, vscale), rel_inf(R32.P.v, R64.P.v, vscale)),
+        'F': (rel_inf(g['F'], R64.P.F, fs), rel_inf(R32.P.F, R64.P.F, fs)),
+        'Jp': (rel_inf(g['Jp'], R64.P.Jp, js), rel_inf(R32.P.Jp, R64.P.Jp, js)),
+    }
+
+
+def start(sc):
+    s = sc.make_solver(use_g2p2g=True)
+    cfg = oracle_config(sc)
+    P64 = O.Particles.seeded(sc.x, sc.material, v=sc.v)
+    win = O.Window.covering(P64.x, cfg.inv_dx, margin=16)
+    return s, O.G2P2GRunner(cfg, P64, win), O.G2P2GRunner(cfg, P64.astype(np.float32), win), win
+
+
+@pytest.mark.parametrize("scene_fn,nsub", [(scenes.smoke_scene, 1), (scenes.smoke_scene, 12),
+                                           (lambda: scenes.four_materials_128(per_cube=8000), 8)])
+def test_g2p2g_substeps_match_oracle(scene_fn, nsub):
+    sc = scene_fn()
+    s, R64, R32, win = start(sc)
+    dt = sc.default_dt
+    for _ in range(nsub):
+        s.substep(dt)
+        R64.step(dt)
+        R32.step(dt)
+    for k, (g, f32) in errors(s, R64, R32, win).items():
+        assert g <= max(TOL[k], 4 * f32), f"{k}: gpu {g:.3g} vs f32-oracle {f32:.3g}"
+
+
+def test_g2p2g_trajectory_100_substeps():
+    sc = scenes.smoke_scene()
+    s, R64, _, _ = start(sc)
+    dt = sc.default_dt
+    for _ in range(100):
+        s.substep(dt)
+        R64.step(dt)
+    x = gpu_particles(s)['x']
+    err = np.linalg.norm(x - R64.P.x) / np.linalg.norm(R64.P.x)
+    assert err < 1e-3, err
+
+
+def test_g2p2g_frames_and_particles_added_between_frames():
+    """step() frames (CUDA graphs from the second frame) and a cube added
+    after them: the new particles skip the gather in their first substep."""
+    sc = scenes.smoke_scene()
+    s = sc.make_solver(use_g2p2g=True)
+    for _ in range(3):
+        s.step(1e-3)
+    s.add_cube((0.4, 0.6, 0.4), (0.1, 0.1, 0.1), s.material_water, velocity=(0.0, -1.0, 0.0))
+    # oracle from the engine's state: particles (old ones first) and its grid
+    cfg = oracle_config(s)
+    st = s.full_state()
+    P = O.Particles(*(st[k].cpu().numpy().astype(np.float64) for k in ('x', 'v', 'C', 'F', 'Jp')),
+                    st['material'].cpu().numpy().astype(np.int32))
+    win = O.Window.covering(P.x, cfg.inv_dx, margin=16)
+    R = O.G2P2GRunner(cfg, P, win)
+    coords, vel = gpu_grid(s.views(), 'grid_vel')
+    gv = np.zeros(tuple(win.W) + (3,))
+    inside = np.all((coords >= win.lo) & (coords < win.lo + win.W), 1)
+    gv[tuple((coords[inside] - win.lo).T)] = vel[inside, :3]
+    R.gv = gv.reshape(-1)
+    R.last_final = s._last_final
+    assert R.last_final < P.n
+    dt = s.default_dt
+    s.substep(dt)
+    R.step(dt)
+    g = gpu_particles(s)
+    assert rel_inf(g['x'], R.P.x, 1.0) < 1e-5
+    assert rel_inf(g['v'], R.P.v, max(np.abs(R.P.v).max(), 1e-3)) < 1e-4
+    new = np.arange(R.last_final, P.n)
+    assert np.allclose(g['v'][new], R.P.v[new], atol=1e-5)

@@ -272,6 +272,9 @@ def run_gb300(args):
     adjoint = None
     if not args.no_adjoint:
         adjoint = run_adjoint_measure()
+    g2p2g = None
+    if not args.no_g2p2g:
+        g2p2g = run_g2p2g_measure(sc)
     pio = mesh = None
     if not args.no_io:
         pio = run_particle_output_measure(solver, peak, peak_kind, rank == 0 and not args.no_cpu)
@@ -317,6 +320,7 @@ def run_gb300(args):
         "cpu_baseline": cpu,
         "batched": batched,
         "fwd_adjoint": adjoint,
+        "g2p2g": g2p2g,
         "particle_output": pio,
         "mesh_emitter": mesh,
     }
@@ -480,6 +484,35 @@ def run_mesh_emitter_measure(peak, peak_kind, with_cpu, reps=5):
         out["cpu_baseline"] = {"value": len(sample) / tc, "unit": "triangles/s", "cores": 1, "kind": "port",
                                "sample": f"{len(sample)} of the triangles through the numpy restatement of "
                                          "Voxelizer.voxelize_triangles on the same 512^3 voxel grid"}
+    return out
+
+
+def run_g2p2g_measure(sc, substeps=50, warmup=5):
+    """The same scene in the fused G2P2G mode (MPMSolver(use_g2p2g=True),
+    engine/mpm_solver.py:363-485): K substeps timed with CUDA events."""
+    import torch
+    s = sc.make_solver(use_g2p2g=True, chunk=512)
+    dt = sc.default_dt
+    s._prepare(dt)
+    for _ in range(warmup):
+        s._launch_substep(dt, -1)
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(substeps):
+        s._launch_substep(dt, -1)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / substeps
+    if int(s._status.item()):
+        raise RuntimeError("device status set during the G2P2G measurement")
+    n = s.n_particles
+    out = {"value": n / (ms / 1e3), "unit": "particle-substeps/s (fused G2P2G mode)", "ms_per_substep": ms,
+           "substeps": substeps, "gpu_launches_per_substep": 8,
+           "note": "use_g2p2g=True semantics (reference :363-485): C not stored, p_mass for every material"}
+    del s
+    torch.cuda.empty_cache()
     return out
 
 
@@ -664,6 +697,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-io", action="store_true", help="skip the particle-output and mesh-emitter measurements")
+    ap.add_argument("--no-g2p2g", action="store_true", help="skip the fused G2P2G-mode measurement")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--e2e-frames", type=int, default=3)
     ap.add_argument("--e2e-substeps", type=int, default=50)

@@ -22,7 +22,7 @@ BUILD_DIR = PKG_DIR / "_build"
 LIB_NAME = "libmpm_gb300.so"
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-SOURCES = ["mpm_kernels.cu", "mpm_adjoint.cu", "mpm_io.cu", "mpm_voxelize.cu"]
+SOURCES = ["mpm_kernels.cu", "mpm_adjoint.cu", "mpm_io.cu", "mpm_voxelize.cu", "mpm_render.cu"]
 
 
 def nvcc_path() -> str:

@@ -272,6 +272,9 @@ def run_gb300(args):
     adjoint = None
     if not args.no_adjoint:
         adjoint = run_adjoint_measure()
+    render = None
+    if not args.no_render:
+        render = run_render_measure(solver, rank == 0 and not args.no_cpu)
     g2p2g = None
     if not args.no_g2p2g:
         g2p2g = run_g2p2g_measure(sc)
@@ -321,6 +324,7 @@ def run_gb300(args):
         "batched": batched,
         "fwd_adjoint": adjoint,
         "g2p2g": g2p2g,
+        "render": render,
         "particle_output": pio,
         "mesh_emitter": mesh,
     }
@@ -516,6 +520,59 @@ def run_g2p2g_measure(sc, substeps=50, warmup=5):
     return out
 
 
+def run_render_measure(solver, with_cpu, spp=8):
+    """The path tracer on the bench scene's particles (renderer.py with the
+    render_particles.py settings at res 512: dx = 1/512, sphere radius
+    0.3/512, shutter 2e-3, 1280 x 720): cell-list build and `spp` samples
+    per pixel timed with CUDA events."""
+    import torch
+
+    from taichi_elements_gb300.renderer import Renderer
+    r = Renderer(dx=1 / 512, sphere_radius=0.3 / 512, shutter_time=2e-3, taichi_logo=False)
+    r.set_camera_pos(3.24, 1.86, -4.57)
+    r.look_at[None] = (0.5, 0.3, 0.5)
+    r.floor_height[None] = -5e-3
+    stream = torch.cuda.current_stream()
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    torch.cuda.synchronize()
+    e0.record(stream)
+    r.initialize_particles_from_solver(solver)
+    e1.record(stream)
+    r.render(spp)
+    e2.record(stream)
+    torch.cuda.synchronize()
+    t_build, t_render = e0.elapsed_time(e1), e1.elapsed_time(e2)
+    npix = r.res[0] * r.res[1]
+    out = {"value": npix * spp / (t_render / 1e3), "unit": "pixel-samples/s (path tracing, device kernel)",
+           "resolution": list(r.res), "spp": spp, "ms_per_spp": t_render / spp, "ms_cell_lists": t_build,
+           "particles": r.num_particles, "listed_particle_cells": r.total_inserted_particles(),
+           "gpu_launches": 2 + spp // 8 + (1 if spp % 8 else 0)}
+    if with_cpu:
+        import numpy as np
+
+        from oracle import renderer_ref as R
+        sel = np.random.default_rng(0).choice(r.num_particles, size=min(r.num_particles, 1000), replace=False)
+        x = r._x[torch.as_tensor(sel, device=r._x.device)].cpu().numpy()
+        v = np.zeros_like(x)
+        rgb = r._rgb[torch.as_tensor(sel, device=r._rgb.device)].cpu().numpy()
+        g = R.Grid(x, r.dx)
+        lists = R.cell_lists(g, x, v, r.sphere_radius, 0.0, motion_blur=False)
+        pos, d = R.camera_rays(r.res, r.camera_pos[None], r.look_at[None], r.up[None], r.fov[None],
+                               np.full(r.res + (2,), 0.5, np.float32))
+        pos, d = pos.reshape(-1, 3)[::4000], d.reshape(-1, 3)[::4000]
+        t0 = time.perf_counter()
+        for q in range(len(pos)):
+            R.next_hit(g, lists, x, v, rgb, np.float32(r.sphere_radius), pos[q], d[q], np.float32(0.0),
+                       np.float32(-5e-3), False, motion_blur=False)
+        tc = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": len(pos) / tc, "unit": "ray hits/s (nearest-hit query only)", "cores": 1,
+                               "kind": "port", "sample": f"{len(pos)} camera rays against 1,000 of the particles "
+                                                         "through the python restatement of next_hit"}
+    del r
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_batched_measure(frames=3, substeps=50):
     """64 independent scenes (grids 32-96^3, 8K-300K particles each) advanced
     by the batched engine in CUDA-graph frames of `substeps` substeps, and the
@@ -698,6 +755,7 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-io", action="store_true", help="skip the particle-output and mesh-emitter measurements")
     ap.add_argument("--no-g2p2g", action="store_true", help="skip the fused G2P2G-mode measurement")
+    ap.add_argument("--no-render", action="store_true", help="skip the path-tracer measurement")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--e2e-frames", type=int, default=3)
     ap.add_argument("--e2e-substeps", type=int, default=50)

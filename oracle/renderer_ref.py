@@ -4,7 +4,8 @@ Follows taichi-dev/taichi_elements engine/renderer.py and
 engine/renderer_utils.py in float32:
 * ``cell_lists``: initialize_particle_grid (:482-517) with
   sphere_aabb_intersect_motion (renderer_utils.py:133-147);
-* ``next_hit``: dda_particle (:297-366), the z = -5.5 plane (:375-380), the
+* ``next_hit``: dda_particle (:297-366) or, for the voxel view, dda_voxel
+  (:217-281) with voxel_color (:146-160), the z = -5.5 plane (:375-380), the
   floor reached by sphere tracing (ray_march :180-191, sdf_normal :193-203,
   sdf_color :205-214 with inside_taichi, renderer_utils.py:164-195);
 * ``render_no_particles``: the path tracer of render (:396-480) vectorised
@@ -189,6 +190,54 @@ def dda_particle(grid, lists, x, v, rgb, radius, eye, d, t, motion_blur):
     return closest, normal, color
 
 
+def voxel_color(pos, inv_dx):
+    p = pos * inv_dx
+    p = p - np.floor(p)
+    count = int(np.sum((p < F(0.1)) | (p > F(1.0) - F(0.1))))
+    f = F(1.0) if count >= 2 else F(0.0)
+    return np.array([0.9, 0.8, 1.0], F) * (F(1.3) - F(1.2) * f)
+
+
+def dda_voxel(grid, lists, eye, d):
+    """renderer.py:217-281: the first cell holding a particle."""
+    d = d.copy()
+    for i in range(3):
+        if abs(d[i]) < F(1e-6):
+            d[i] = F(1e-6)
+    rinv = F(1.0) / d
+    rs = np.where(d > 0, 1, -1)
+    hit, normal, color = INF, np.zeros(3, F), np.zeros(3, F)
+    inter, near, _ = ray_aabb(grid.bmin, grid.bmax, eye, d)
+    if not inter:
+        return hit, normal, color
+    near = max(F(0.0), near)
+    pos = eye + d * (near + F(5.0) * EPS)
+    o = grid.inv_dx * pos
+    ip = np.floor(o).astype(np.int64)
+    dis = (ip.astype(F) - o + F(0.5) + rs.astype(F) * F(0.5)) * rinv
+    for _ in range(int(grid.nc.sum()) + 8):
+        occupied = tuple(int(c) for c in ip) in lists
+        inside = grid.inside(*ip)
+        if occupied:
+            mini = ((ip.astype(F) - o + F(0.5) - rs.astype(F) * F(0.5)) * rinv).max()
+            hit = F(mini * grid.dx + near)
+            color = voxel_color(eye + hit * d, grid.inv_dx)
+            break
+        if dis[0] <= dis[1] and dis[0] < dis[2]:
+            m = 0
+        elif dis[1] <= dis[0] and dis[1] <= dis[2]:
+            m = 1
+        else:
+            m = 2
+        dis[m] += F(rs[m]) * rinv[m]
+        ip[m] += rs[m]
+        normal = np.zeros(3, F)
+        normal[m] = -rs[m]
+        if not inside:
+            break
+    return hit, normal, color
+
+
 def ray_march(p, d, floor_height):
     dist, j = F(0.0), 0
     while j < 200 and (p[1] + dist * d[1]) - floor_height > F(1e-8) and dist < DIST_LIMIT:
@@ -204,8 +253,11 @@ def floor_color(p, taichi_logo):
     return scale * np.array([0.3, 0.5, 0.7], F)
 
 
-def next_hit(grid, lists, x, v, rgb, radius, pos, d, t, floor_height, taichi_logo, motion_blur=True):
-    closest, normal, color = dda_particle(grid, lists, x, v, rgb, radius, pos, d, t, motion_blur)
+def next_hit(grid, lists, x, v, rgb, radius, pos, d, t, floor_height, taichi_logo, motion_blur=True, voxel=False):
+    if voxel:
+        closest, normal, color = dda_voxel(grid, lists, pos, d)
+    else:
+        closest, normal, color = dda_particle(grid, lists, x, v, rgb, radius, pos, d, t, motion_blur)
     if d[2] != 0:
         rc = -(pos[2] + F(5.5)) / d[2]
         if 0 < rc < closest:

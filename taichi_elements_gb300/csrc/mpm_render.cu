@@ -44,6 +44,8 @@ struct RenderScene {
   float floor_height;
   int taichi_logo;
   float light_dir[3], light_noise, light_color[3];
+  int render_voxel;  // the voxel view: cells holding particles drawn as cubes
+  int pad_;
   uint64_t seed;
 };
 
@@ -295,6 +297,66 @@ __device__ Hit dda_particle(const RenderScene &S, const Cells &G, V3 eye, V3 d, 
   return h;
 }
 
+// renderer.py:146-160: cube edges drawn darker
+__device__ __forceinline__ V3 voxel_color(const RenderScene &S, V3 pos) {
+  V3 p = S.inv_dx * pos;
+  p = v3(p.x - floorf(p.x), p.y - floorf(p.y), p.z - floorf(p.z));
+  const float b = 0.1f;  // voxel_edges
+  int count = 0;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+    if (comp(p, i) < b || comp(p, i) > 1.0f - b) ++count;
+  const float f = count >= 2 ? 1.0f : 0.0f;
+  return (1.3f - 1.2f * f) * v3(0.9f, 0.8f, 1.0f);
+}
+
+// renderer.py:217-281 (render_voxel = True): DDA to the first cell holding a
+// particle; the normal is that of the last face crossed (zero when the first
+// cell sampled is already occupied, as in the reference)
+__device__ Hit dda_voxel(const RenderScene &S, const Cells &G, V3 eye, V3 d) {
+  Hit h{kInf, v3(0.f, 0.f, 0.f), v3(0.f, 0.f, 0.f)};
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+    if (fabsf(comp(d, i)) < 1e-6f) set_comp(d, i, 1e-6f);
+  const V3 rinv = v3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+  const int rs[3] = {d.x > 0.0f ? 1 : -1, d.y > 0.0f ? 1 : -1, d.z > 0.0f ? 1 : -1};
+  const V3 bmin = v3(S.bbox_min[0], S.bbox_min[1], S.bbox_min[2]);
+  const V3 bmax = v3(S.bbox_max[0], S.bbox_max[1], S.bbox_max[2]);
+  float near_int, far_int;
+  if (!ray_aabb_intersection(bmin, bmax, eye, d, near_int, far_int)) return h;
+  near_int = fmaxf(0.0f, near_int);
+  const V3 pos = eye + (near_int + 5.0f * kEps) * d;
+  const V3 o = S.inv_dx * pos;
+  int ip[3] = {(int)floorf(o.x), (int)floorf(o.y), (int)floorf(o.z)};
+  float dis[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) dis[i] = ((float)ip[i] - comp(o, i) + 0.5f + (float)rs[i] * 0.5f) * comp(rinv, i);
+  const int max_steps = S.nc[0] + S.nc[1] + S.nc[2] + 8;
+  for (int step = 0; step < max_steps; ++step) {
+    const int64_t c = cell_index(S, ip[0], ip[1], ip[2]);
+    const bool occupied = c >= 0 && G.count[c] > 0;
+    const bool inside = inside_particle_grid(S, ip[0], ip[1], ip[2]);
+    if (occupied) {
+      float mini = -kInf;
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+        mini = fmaxf(mini, ((float)ip[i] - comp(o, i) + 0.5f - (float)rs[i] * 0.5f) * comp(rinv, i));
+      h.dist = mini * S.dx + near_int;
+      h.color = voxel_color(S, eye + h.dist * d);
+      break;
+    }
+    int m;
+    if (dis[0] <= dis[1] && dis[0] < dis[2]) m = 0;
+    else if (dis[1] <= dis[0] && dis[1] <= dis[2]) m = 1;
+    else m = 2;
+    dis[m] += (float)rs[m] * comp(rinv, m);
+    ip[m] += rs[m];
+    h.normal = v3(m == 0 ? -(float)rs[0] : 0.f, m == 1 ? -(float)rs[1] : 0.f, m == 2 ? -(float)rs[2] : 0.f);
+    if (!inside) break;  // the reference steps once more before it stops
+  }
+  return h;
+}
+
 // floor supporter (renderer.py:162-178 with supporter = 2)
 __device__ __forceinline__ float sdf(const RenderScene &S, V3 o) { return o.y - S.floor_height; }
 
@@ -350,7 +412,7 @@ __device__ __forceinline__ V3 sdf_color(const RenderScene &S, V3 p) {
 
 // renderer.py:368-386
 __device__ Hit next_hit(const RenderScene &S, const Cells &G, V3 pos, V3 d, float t) {
-  Hit h = dda_particle(S, G, pos, d, t);
+  Hit h = S.render_voxel ? dda_voxel(S, G, pos, d) : dda_particle(S, G, pos, d, t);
   if (d.z != 0.0f) {
     const float rc = -(pos.z + 5.5f) / d.z;
     if (rc > 0.0f && rc < h.dist) {

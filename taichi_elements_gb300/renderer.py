@@ -7,8 +7,8 @@
 ``total_inserted_particles``, ``reset`` and ``render_frame(spp)`` returning
 the (res[0], res[1], 3) float32 image; the work runs in the kernels of
 csrc/mpm_render.cu.  ``initialize_particles_from_solver`` renders a running
-MPMSolver's particles straight from device memory.  Only the particle view is
-provided (``render_voxel=False``, the reference's default).
+MPMSolver's particles straight from device memory.  ``render_voxel=True``
+draws the occupied cells as cubes (the reference's voxel view).
 """
 from __future__ import annotations
 
@@ -41,7 +41,8 @@ class RenderScene(ctypes.Structure):
         ("cam", ctypes.c_float * 3), ("look_at", ctypes.c_float * 3), ("up", ctypes.c_float * 3),
         ("fov", ctypes.c_float), ("res", ctypes.c_int32 * 2), ("floor_height", ctypes.c_float),
         ("taichi_logo", ctypes.c_int32), ("light_dir", ctypes.c_float * 3), ("light_noise", ctypes.c_float),
-        ("light_color", ctypes.c_float * 3), ("seed", ctypes.c_uint64),
+        ("light_color", ctypes.c_float * 3), ("render_voxel", ctypes.c_int32), ("pad_", ctypes.c_int32),
+        ("seed", ctypes.c_uint64),
     ]
 
 
@@ -67,8 +68,6 @@ class Renderer:
 
     def __init__(self, dx=1 / 1024, sphere_radius=0.3 / 1024, render_voxel=False, shutter_time=1e-3, taichi_logo=True,
                  max_num_particles_million=128, res=RES, seed=0, device=None):
-        if render_voxel:
-            raise NotImplementedError("the voxel view (render_voxel=True) is not provided; the particle view is")
         assert sphere_radius * 2 < dx
         self.device = torch.device(device if device is not None else "cuda")
         self._lib = _lib.load()
@@ -78,6 +77,8 @@ class Renderer:
         self.vignette_radius = 0.0
         self.vignette_center = [0.5, 0.5]
         self.taichi_logo = taichi_logo
+        self.render_voxel = bool(render_voxel)
+        self.voxel_edges = 0.1
         self.shutter_time = shutter_time
         self.enable_motion_blur = self.shutter_time != 0.0
         self.dx = dx
@@ -143,6 +144,7 @@ class Renderer:
         s.floor_height = float(self.floor_height[None])
         s.taichi_logo = int(bool(self.taichi_logo))
         s.light_noise = LIGHT_DIRECTION_NOISE
+        s.render_voxel = int(self.render_voxel)
         s.seed = self.seed
         return s
 

@@ -22,8 +22,9 @@ def particle_scene(n, seed=0, blur=True):
     return x, v, rgb
 
 
-def make(x, v, rgb, dx=1 / 64, shutter=1e-3, res=(48, 27), logo=True):
-    r = Renderer(dx=dx, sphere_radius=0.3 * dx, shutter_time=shutter, taichi_logo=logo, res=res, seed=1)
+def make(x, v, rgb, dx=1 / 64, shutter=1e-3, res=(32, 18), logo=True, voxel=False):
+    r = Renderer(dx=dx, sphere_radius=0.3 * dx, shutter_time=shutter, taichi_logo=logo, res=res, seed=1,
+                 render_voxel=voxel)
     r.set_camera_pos(0.45, 0.45, 1.6)
     r.look_at[None] = (0.45, 0.12, 0.45)
     r.floor_height[None] = 0.0
@@ -32,7 +33,7 @@ def make(x, v, rgb, dx=1 / 64, shutter=1e-3, res=(48, 27), logo=True):
 
 
 def test_cell_lists_match_restatement():
-    x, v, rgb = particle_scene(500, seed=1)
+    x, v, rgb = particle_scene(300, seed=1)
     r = make(x, v, rgb, shutter=2e-2)  # long shutter: particles span several cells
     g = R.Grid(x, r.dx)
     assert np.array_equal(g.c0, r._cells[0]) and np.array_equal(g.nc, r._cells[1])
@@ -41,7 +42,7 @@ def test_cell_lists_match_restatement():
     for (i, j, k), ps in lists.items():
         want[((i - g.c0[0]) * g.nc[1] + (j - g.c0[1])) * g.nc[2] + (k - g.c0[2])] = len(ps)
     got = r._count.cpu().numpy()
-    assert got.sum() == want.sum() > 500
+    assert got.sum() == want.sum() > 300
     assert (got != want).mean() < 1e-3
     # the lists hold the right particles
     cnt, start, lst = r._count.cpu().numpy(), r._start.cpu().numpy(), r._list.cpu().numpy()
@@ -51,9 +52,10 @@ def test_cell_lists_match_restatement():
             assert sorted(lst[start[c]:start[c] + cnt[c]]) == sorted(ps)
 
 
-def test_first_hits_match_restatement():
+@pytest.mark.parametrize("voxel", [False, True])
+def test_first_hits_match_restatement(voxel):
     x, v, rgb = particle_scene(3000, seed=2)
-    r = make(x, v, rgb)
+    r = make(x, v, rgb, voxel=voxel)
     g = R.Grid(x, r.dx)
     lists = R.cell_lists(g, x, v, r.sphere_radius, r.shutter_time)
     pos, d = R.camera_rays(r.res, r.camera_pos[None], r.look_at[None], r.up[None], r.fov[None],
@@ -63,7 +65,8 @@ def test_first_hits_match_restatement():
     got = r.first_hits(pos, d, t)
     agree, close = 0, 0
     for q in range(len(pos)):
-        dist, nrm, col = R.next_hit(g, lists, x, v, rgb, F(r.sphere_radius), pos[q], d[q], F(t), F(0.0), True)
+        dist, nrm, col = R.next_hit(g, lists, x, v, rgb, F(r.sphere_radius), pos[q], d[q], F(t), F(0.0), True,
+                                    voxel=voxel)
         same = np.allclose(got[q, 1:4], nrm, atol=1e-3) and np.allclose(got[q, 4:7], col, atol=1e-5)
         agree += same
         close += same and abs(got[q, 0] - dist) <= 1e-4 * max(1.0, abs(dist))
@@ -84,7 +87,7 @@ def test_light_transport_matches_restatement_in_distribution():
     r.render(gpu_spp)
     gmean = r.color_buffer.cpu().numpy() / gpu_spp
     rng = np.random.default_rng(0)
-    n_spp = 96
+    n_spp = 64
     s1 = np.zeros(r.res + (3,))
     s2 = np.zeros(r.res + (3,))
     for _ in range(n_spp):

@@ -92,7 +92,11 @@ __device__ __forceinline__ void bin_one(const MpmParams &P, const MpmParams *tab
   // (the blocks the reference's sparse grid activates in P2G, :582-584).
   const int need = ((b.b[0] & 3) >= 2 ? 4 : 0) | ((b.b[1] & 3) >= 2 ? 2 : 0) | ((b.b[2] & 3) >= 2 ? 1 : 0);
   const int mask = kNeighbourMask[need];
-  if ((w.blk_flag[blin] & mask) != mask) atomicOr(&w.blk_flag[blin], mask);
+  // lanes of a warp mostly share a block: one fire-and-forget OR per block
+  const unsigned act = __activemask();
+  const unsigned same = __match_any_sync(act, blin);
+  const int all = (int)__reduce_or_sync(same, (unsigned)mask);
+  if ((threadIdx.x & 31) == __ffs(same) - 1) atomicOr(&w.blk_flag[blin], all);
   w.cellkey[i] = key;
 }
 

@@ -305,7 +305,9 @@ int mpm_voxel_seed_emit(const int32_t *voxels, int32_t rx, int32_t ry, int32_t r
  * (int64[cells], exclusive) and sizes `list` (int32[list_len]);
  * mpm_render_cell_fill writes the particle indices (`fill`, int32[cells],
  * zeroed).  x, v: float32[n * 3] (v may be NULL: no motion blur); rgb:
- * uint8[n * 3].  mpm_render_samples adds `spp` path-traced samples
+ * uint8[n * 3].  mpm_render_occupancy packs one bit per cell (count > 0)
+ * into `occ` (uint32[(cells + 31) / 32]), which the tracing calls read
+ * before touching a cell's list.  mpm_render_samples adds `spp` path-traced samples
  * (sample indices sample0 ..) of every pixel to color_buffer
  * (float32[res0 * res1 * 3], pixel (u, v) at (u * res1 + v) * 3);
  * mpm_render_tonemap writes the displayed image (vignette, exposure,
@@ -317,15 +319,16 @@ int mpm_render_cell_count(const void *scene, const float *x, const float *v, int
                           void *stream);
 int mpm_render_cell_fill(const void *scene, const float *x, const float *v, int64_t n, const int64_t *start,
                          int32_t *fill, int64_t list_len, int32_t *list, void *stream);
-int mpm_render_samples(const void *scene, const int64_t *start, const int32_t *count, const int32_t *list,
-                       const float *x, const float *v, const uint8_t *rgb, int32_t sample0, int32_t spp,
-                       float *color_buffer, void *stream);
+int mpm_render_occupancy(const int32_t *count, int64_t ncells, uint32_t *occ, void *stream);
+int mpm_render_samples(const void *scene, const uint32_t *occ, const int64_t *start, const int32_t *count,
+                       const int32_t *list, const float *x, const float *v, const uint8_t *rgb, int32_t sample0,
+                       int32_t spp, float *color_buffer, void *stream);
 int mpm_render_tonemap(int32_t rx, int32_t ry, const float *color_buffer, float vignette_strength,
                        float vignette_radius, float vcx, float vcy, float exposure, int32_t samples, float *img,
                        void *stream);
-int mpm_render_first_hits(const void *scene, const int64_t *start, const int32_t *count, const int32_t *list,
-                          const float *x, const float *v, const uint8_t *rgb, const float *orig, const float *dir,
-                          int64_t nrays, float t, float *out, void *stream);
+int mpm_render_first_hits(const void *scene, const uint32_t *occ, const int64_t *start, const int32_t *count,
+                          const int32_t *list, const float *x, const float *v, const uint8_t *rgb, const float *orig,
+                          const float *dir, int64_t nrays, float t, float *out, void *stream);
 
 /* Pointer to the device status word inside the workspace (uint32). */
 int mpm_status_ptr(const MpmParams *p, void *ws, int64_t cap, uint32_t **status_out);

@@ -115,9 +115,10 @@ SIGNATURES = {
     "mpm_render_scene_bytes": [],
     "mpm_render_cell_count": [_v, _v, _v, _i64, _v, _v],
     "mpm_render_cell_fill": [_v, _v, _v, _i64, _v, _v, _i64, _v, _v],
-    "mpm_render_samples": [_v, _v, _v, _v, _v, _v, _v, _i32, _i32, _v, _v],
+    "mpm_render_occupancy": [_v, _i64, _v, _v],
+    "mpm_render_samples": [_v, _v, _v, _v, _v, _v, _v, _v, _i32, _i32, _v, _v],
     "mpm_render_tonemap": [_i32, _i32, _v, _f, _f, _f, _f, _f, _i32, _v, _v],
-    "mpm_render_first_hits": [_v, _v, _v, _v, _v, _v, _v, _v, _v, _i64, _f, _v, _v],
+    "mpm_render_first_hits": [_v, _v, _v, _v, _v, _v, _v, _v, _v, _v, _i64, _f, _v, _v],
     "mpm_voxelize": [_v, _i64, _i32, _i32, _i32, ctypes.c_double, _i32, _v, _v],
     "mpm_voxel_seed_count": [_v, _i32, _i32, _i32, _i32, _i32, _i32, _i32, ctypes.c_uint64, _v, _v],
     "mpm_voxel_seed_emit": [_v, _i32, _i32, _i32, _i32, _i32, _i32, _i32, ctypes.c_uint64, _f, _f, _f, _f, _v,

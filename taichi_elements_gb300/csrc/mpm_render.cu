@@ -193,6 +193,7 @@ struct Hit {
 };
 
 struct Cells {
+  const uint32_t *occ;  // one bit per cell: the cell lists a particle (fits in L2)
   const int64_t *start;
   const int32_t *count;
   const int32_t *list;
@@ -271,7 +272,7 @@ __device__ Hit dda_particle(const RenderScene &S, const Cells &G, V3 eye, V3 d, 
       break;
     }
     const int64_t c = cell_index(S, ip[0], ip[1], ip[2]);
-    if (c >= 0) {
+    if (c >= 0 && ((G.occ[c >> 5] >> (c & 31)) & 1u)) {
       const int64_t s0 = G.start[c];
       const int cnt = G.count[c];
       for (int q = 0; q < cnt; ++q) {
@@ -334,7 +335,7 @@ __device__ Hit dda_voxel(const RenderScene &S, const Cells &G, V3 eye, V3 d) {
   const int max_steps = S.nc[0] + S.nc[1] + S.nc[2] + 8;
   for (int step = 0; step < max_steps; ++step) {
     const int64_t c = cell_index(S, ip[0], ip[1], ip[2]);
-    const bool occupied = c >= 0 && G.count[c] > 0;
+    const bool occupied = c >= 0 && ((G.occ[c >> 5] >> (c & 31)) & 1u);
     const bool inside = inside_particle_grid(S, ip[0], ip[1], ip[2]);
     if (occupied) {
       float mini = -kInf;
@@ -498,6 +499,14 @@ __global__ __launch_bounds__(kRenderThreads) void k_render(RenderScene S, Cells 
   color_buffer[pix * 3 + 2] += acc.z;
 }
 
+// occupancy bits of the cell counts
+__global__ void k_occupancy(const int32_t *__restrict__ count, int64_t ncells, uint32_t *__restrict__ occ) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool on = c < ncells && count[c] > 0;
+  const unsigned bits = __ballot_sync(0xffffffffu, on);
+  if ((threadIdx.x & 31) == 0 && c < ncells) occ[c >> 5] = bits;
+}
+
 // renderer.py:519-531
 __global__ void k_tonemap(int rx, int ry, const float *__restrict__ color_buffer, float vignette_strength,
                           float vignette_radius, float vcx, float vcy, float exposure, int samples,
@@ -558,14 +567,22 @@ int mpm_render_cell_fill(const void *scene, const float *x, const float *v, int6
   return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_E_CUDA;
 }
 
-int mpm_render_samples(const void *scene, const int64_t *start, const int32_t *count, const int32_t *list,
-                       const float *x, const float *v, const uint8_t *rgb, int32_t sample0, int32_t spp,
-                       float *color_buffer, void *stream) {
+int mpm_render_occupancy(const int32_t *count, int64_t ncells, uint32_t *occ, void *stream) {
+  if (!count || !occ || ncells < 0) return MPM_E_INVALID;
+  if (ncells == 0) return MPM_OK;
+  k_occupancy<<<(unsigned)((ncells + 255) / 256), 256, 0, (cudaStream_t)stream>>>(count, ncells, occ);
+  return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_E_CUDA;
+}
+
+int mpm_render_samples(const void *scene, const uint32_t *occ, const int64_t *start, const int32_t *count,
+                       const int32_t *list, const float *x, const float *v, const uint8_t *rgb, int32_t sample0,
+                       int32_t spp, float *color_buffer, void *stream) {
   const RenderScene *S = (const RenderScene *)scene;
-  if (!scene_ok(S) || !start || !count || !list || !x || !rgb || !color_buffer || spp < 0) return MPM_E_INVALID;
+  if (!scene_ok(S) || !occ || !start || !count || !list || !x || !rgb || !color_buffer || spp < 0)
+    return MPM_E_INVALID;
   if (spp == 0) return MPM_OK;
   const int64_t npix = (int64_t)S->res[0] * S->res[1];
-  Cells G{start, count, list, x, v, rgb};
+  Cells G{occ, start, count, list, x, v, rgb};
   k_render<<<(unsigned)((npix + kRenderThreads - 1) / kRenderThreads), kRenderThreads, 0, (cudaStream_t)stream>>>(
       *S, G, sample0, spp, color_buffer);
   return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_E_CUDA;
@@ -581,14 +598,14 @@ int mpm_render_tonemap(int32_t rx, int32_t ry, const float *color_buffer, float 
   return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_E_CUDA;
 }
 
-int mpm_render_first_hits(const void *scene, const int64_t *start, const int32_t *count, const int32_t *list,
-                          const float *x, const float *v, const uint8_t *rgb, const float *orig, const float *dir,
-                          int64_t nrays, float t, float *out, void *stream) {
+int mpm_render_first_hits(const void *scene, const uint32_t *occ, const int64_t *start, const int32_t *count,
+                          const int32_t *list, const float *x, const float *v, const uint8_t *rgb, const float *orig,
+                          const float *dir, int64_t nrays, float t, float *out, void *stream) {
   const RenderScene *S = (const RenderScene *)scene;
-  if (!scene_ok(S) || !start || !count || !list || !x || !rgb || !orig || !dir || !out || nrays < 0)
+  if (!scene_ok(S) || !occ || !start || !count || !list || !x || !rgb || !orig || !dir || !out || nrays < 0)
     return MPM_E_INVALID;
   if (nrays == 0) return MPM_OK;
-  Cells G{start, count, list, x, v, rgb};
+  Cells G{occ, start, count, list, x, v, rgb};
   k_first_hits<<<(unsigned)((nrays + 127) / 128), 128, 0, (cudaStream_t)stream>>>(*S, G, orig, dir, nrays, t, out);
   return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_E_CUDA;
 }

@@ -96,7 +96,7 @@ class Renderer:
         self.num_particles = 0
         self._samples = 0
         self._x = self._v = self._rgb = None
-        self._start = self._count = self._list = None
+        self._start = self._count = self._list = self._occ = None
         self._cells = None
         self.set_up(0, 1, 0)
         self.set_fov(0.23)
@@ -120,7 +120,7 @@ class Renderer:
 
     def reset(self):
         self._x = self._v = self._rgb = None
-        self._start = self._count = self._list = None
+        self._start = self._count = self._list = self._occ = None
         self.num_particles = 0
         self.color_buffer.zero_()
         self._samples = 0
@@ -186,7 +186,10 @@ class Renderer:
         _lib.check(self._lib.mpm_render_cell_fill(ctypes.byref(scene), x.data_ptr(), vp, n, start.data_ptr(),
                                                   fill.data_ptr(), total, lst.data_ptr(), self.stream),
                    "mpm_render_cell_fill")
-        self._start, self._count, self._list = start, count, lst
+        occ = torch.empty((ncell + 31) // 32, dtype=torch.int32, device=self.device)
+        _lib.check(self._lib.mpm_render_occupancy(count.data_ptr(), ncell, occ.data_ptr(), self.stream),
+                   "mpm_render_occupancy")
+        self._start, self._count, self._list, self._occ = start, count, lst, occ
 
     def initialize_particles_from_taichi_elements(self, particle_fn):
         """renderer.py:574-601: a quantised frame written by write_particles."""
@@ -217,7 +220,8 @@ class Renderer:
             raise RuntimeError("no particles: call initialize_particles* first")
         scene = self._scene()
         vp = self._v.data_ptr() if self._v is not None else None
-        _lib.check(self._lib.mpm_render_samples(ctypes.byref(scene), self._start.data_ptr(), self._count.data_ptr(),
+        _lib.check(self._lib.mpm_render_samples(ctypes.byref(scene), self._occ.data_ptr(), self._start.data_ptr(),
+                                                self._count.data_ptr(),
                                                 self._list.data_ptr(), self._x.data_ptr(), vp, self._rgb.data_ptr(),
                                                 self._samples, int(spp), self.color_buffer.data_ptr(), self.stream),
                    "mpm_render_samples")
@@ -250,7 +254,8 @@ class Renderer:
         out = torch.empty((o.shape[0], 7), dtype=torch.float32, device=self.device)
         scene = self._scene()
         vp = self._v.data_ptr() if self._v is not None else None
-        _lib.check(self._lib.mpm_render_first_hits(ctypes.byref(scene), self._start.data_ptr(), self._count.data_ptr(),
+        _lib.check(self._lib.mpm_render_first_hits(ctypes.byref(scene), self._occ.data_ptr(), self._start.data_ptr(),
+                                                   self._count.data_ptr(),
                                                    self._list.data_ptr(), self._x.data_ptr(), vp, self._rgb.data_ptr(),
                                                    o.data_ptr(), d.data_ptr(), o.shape[0], float(t), out.data_ptr(),
                                                    self.stream), "mpm_render_first_hits")

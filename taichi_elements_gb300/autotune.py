@@ -53,7 +53,7 @@ def _save_file():
             pass
 
 
-def time_chunks(solver, candidates=CANDIDATES, substeps=4, dt=None):
+def time_chunks(solver, candidates=CANDIDATES, substeps=8, dt=None):
     """Milliseconds per substep for each candidate chunk, measured on a copy."""
     solver._prepare(dt or solver.default_dt)
     dt = float(dt or solver.default_dt)
@@ -90,7 +90,7 @@ def time_chunks(solver, candidates=CANDIDATES, substeps=4, dt=None):
     return out
 
 
-def tune_chunk(solver, candidates=CANDIDATES, substeps=4) -> int:
+def tune_chunk(solver, candidates=CANDIDATES, substeps=8) -> int:
     """Set solver.chunk to the fastest candidate (cached per shape)."""
     with _lock:
         if not _cache:

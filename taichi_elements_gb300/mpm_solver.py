@@ -508,12 +508,20 @@ class MPMSolver:
         num_particles = int(num_particles)
         if num_particles == 0:
             return
-        x = torch.as_tensor(np.asarray(pos[:num_particles], dtype=np.float32)).reshape(-1, 3)
-        v = torch.as_tensor(np.asarray(vel[:num_particles], dtype=np.float32)).reshape(-1, 3)
-        m = torch.as_tensor(np.asarray(material[:num_particles]).astype(np.int32))
-        c = torch.as_tensor(np.asarray(color[:num_particles]).astype(np.int64).astype(np.int32))
+
+        def dev(a, dtype):
+            # to the device first: conversions and the bounds run there
+            a = np.asarray(a[:num_particles])
+            t = torch.from_numpy(np.ascontiguousarray(a))
+            return t.to(self.device).to(dtype)
+
+        x = dev(pos, torch.float32).reshape(-1, 3)
+        v = dev(vel, torch.float32).reshape(-1, 3)
+        m = dev(material, torch.int32)
+        # colours wrap to int32 like the reference's i32 field
+        c = dev(color, torch.int64).to(torch.int32) if np.asarray(color).dtype != np.int32 else dev(color, torch.int32)
         self._note_region(*self._finite_bounds(x))
-        self._append(x.to(self.device), m, c, v, E=None)
+        self._append(x, m, c, v, E=None)
 
     def add_mesh(self, triangles, material, color=0xFFFFFF, sample_density=None, velocity=None, translation=None,
                  emmiter_id=0):

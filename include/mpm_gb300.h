@@ -330,6 +330,12 @@ int mpm_render_first_hits(const void *scene, const uint32_t *occ, const int64_t 
                           const int32_t *list, const float *x, const float *v, const uint8_t *rgb, const float *orig,
                           const float *dir, int64_t nrays, float t, float *out, void *stream);
 
+/* compute_max_grid_velocity (engine/mpm_solver.py:737-746): raises *out
+ * (device float, zeroed by the caller) to the largest |v_d| over the nodes of
+ * the grid-active blocks of the last substep (0 before the first).  Used by
+ * the adaptive time step (use_adaptive_dt, :761-766). */
+int mpm_max_grid_velocity(const MpmParams *p, void *ws, int64_t cap, float *out, void *stream);
+
 /* Pointer to the device status word inside the workspace (uint32). */
 int mpm_status_ptr(const MpmParams *p, void *ws, int64_t cap, uint32_t **status_out);
 

@@ -129,6 +129,7 @@ SIGNATURES = {
     "mpm_batch_substep": [_P, _v, _v, _i64, _i64, _v, _v, _v, _v],
     "mpm_gather_rows": [_v, _i64, _i64, _i32, _i32, _v, _v],
     "mpm_status_ptr": [_P, _v, _i64, ctypes.POINTER(ctypes.c_void_p)],
+    "mpm_max_grid_velocity": [_P, _v, _i64, _v, _v],
     "mpm_views": [_P, _v, _i64, ctypes.POINTER(MpmViews)],
 }
 

@@ -872,6 +872,23 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_g2p2g(const M
   }
 }
 
+// compute_max_grid_velocity (engine/mpm_solver.py:737-746): the largest |v_d|
+// over the nodes of the grid-active blocks of the last substep; *out (a
+// non-negative float) is raised with an integer atomic max
+__global__ __launch_bounds__(256) void k_max_grid_velocity(const MpmParams P, const Ws w, float *out) {
+  const int ng = w.counters[1];
+  const int64_t total = (int64_t)ng * kBlockCells;
+  float m = 0.0f;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const float4 g = w.grid_vel[(int64_t)w.gblocks[t >> 6] * kBlockCells + (t & 63)];
+    m = fmaxf(m, fmaxf(fabsf(g.x), fmaxf(fabsf(g.y), fabsf(g.z))));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax((int *)out, __float_as_int(m));
+}
+
 __global__ void k_gather_rows(const float *__restrict__ ps, int64_t cap, int64_t n, int row0, int ncols,
                               float *__restrict__ out) {
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1173,6 +1190,16 @@ int mpm_substep_noalloc(const MpmParams *p, int64_t cap, int64_t n, const float 
     k_grid<false><<<di->sms * 8, 256, 0, s>>>(*p, nullptr, w, dt);
     k_g2p<false><<<di->g2p_ctas, kG2PThreads, 0, s>>>(*p, nullptr, w, nxt, cap, dt, maxv_out);
   }
+  return last_error();
+}
+
+int mpm_max_grid_velocity(const MpmParams *p, void *ws, int64_t cap, float *out, void *stream) {
+  if (!params_ok(p) || !ws || !out) return MPM_E_INVALID;
+  const DevInfo *di = dev_info();
+  if (!di) return MPM_E_CUDA;
+  Ws w;
+  ws_layout(*p, cap, (char *)ws, &w);
+  k_max_grid_velocity<<<di->sms * 4, 256, 0, (cudaStream_t)stream>>>(*p, w, out);
   return last_error();
 }
 

@@ -102,8 +102,6 @@ class MPMSolver:
             raise NotImplementedError("quantised particle storage (quant=True) is not implemented")
         if not support_plasticity:
             raise NotImplementedError("support_plasticity=False is not implemented")
-        if use_adaptive_dt:
-            raise NotImplementedError("adaptive dt (use_adaptive_dt=True) is not implemented")
 
         self.device = torch.device(device if device is not None else "cuda")
         if self.device.type != "cuda" or not torch.cuda.is_available():
@@ -682,17 +680,26 @@ class MPMSolver:
             from .autotune import tune_chunk
             tune_chunk(self)
             self._tuned = True
-        if self.n_particles > 0:
+        if self.use_adaptive_dt:
+            dts = self._adaptive_frame(frame_dt, dt)
+            count = len(dts)
+            maxv = self._maxv[:count].cpu().numpy() if self.n_particles > 0 else np.zeros(count, np.float32)
+            if self.n_particles > 0:
+                self._check_status()
+        elif self.n_particles > 0:
             self._run_frame(count, dt)
             maxv = self._maxv[:count].cpu().numpy()
             self._check_status()
+            dts = [dt] * count
         else:
             maxv = np.zeros(count, dtype=np.float32)
+            dts = [dt] * count
         for s in range(count):
             self.total_substeps += 1
-            self.t += dt
+            self.t += dts[s]
             if smry_writer is not None:
-                smry_writer.add_scalar("substep_max_CFL", float(maxv[s]) * dt / self.dx, self.total_substeps)
+                smry_writer.add_scalar("substep_max_CFL", float(maxv[s]) * dts[s] / self.dx, self.total_substeps)
+        dt = dts[-1] if dts else dt
         if count:
             self.all_time_max_velocity = max(self.all_time_max_velocity, float(maxv.max()))
         if print_stat:
@@ -701,6 +708,40 @@ class MPMSolver:
             print(f'num particles={self.n_particles}')
             print(f'  frame time {time.time() - begin_t:.3f} s')
             print(f'  substep time {1000 * (time.time() - begin_t) / max(1, self.total_substeps - begin_substep):.3f} ms')
+
+    def _max_grid_velocity(self) -> float:
+        """compute_max_grid_velocity (engine/mpm_solver.py:737-746) of the
+        last substep's grid (0 before the first)."""
+        if self._ws is None:
+            return 0.0
+        out = torch.zeros(1, dtype=torch.float32, device=self.device)
+        p = self.params
+        _lib.check(self._lib.mpm_max_grid_velocity(ctypes.byref(p), _ptr(self._ws), self._cap, _ptr(out),
+                                                   self.stream), "mpm_max_grid_velocity")
+        return float(out.item())
+
+    def _adaptive_frame(self, frame_dt: float, dt: float):
+        """The adaptive substep loop of engine/mpm_solver.py:756-766: before
+        each substep dt = min(dt, allowed_cfl * dx / (max grid |v| + 1e-6),
+        time left); one host round trip per substep, no CUDA graph."""
+        dts = []
+        frame_time_left = frame_dt
+        if frame_dt / self.default_dt + 2 > self._maxv.numel():
+            self._maxv = torch.zeros(int(frame_dt / self.default_dt) + 1024, dtype=torch.float32,
+                                     device=self.device)
+        self._maxv.zero_()
+        while frame_time_left > 0:
+            max_grid_v = self._max_grid_velocity()
+            cfl_dt = self.g2p2g_allowed_cfl * self.dx / (max_grid_v + 1e-6)
+            dt = min(dt, cfl_dt, frame_time_left)
+            frame_time_left -= dt
+            if len(dts) >= self._maxv.numel():  # a collapsing dt: grow the per-substep record
+                self._maxv = torch.cat([self._maxv, torch.zeros_like(self._maxv)])
+            if self.n_particles > 0:
+                self._launch_substep(dt, len(dts))
+            dts.append(dt)
+        self.last_frame_dts = dts
+        return dts
 
     # --------------------------------------------------------- readback ---
 

@@ -121,4 +121,4 @@ def test_unsupported_flags_raise():
     with pytest.raises(NotImplementedError):
         MPMSolver((16, 16, 16), quant=True)
     with pytest.raises(NotImplementedError):
-        MPMSolver((16, 16, 16), use_adaptive_dt=True)
+        MPMSolver((16, 16, 16), support_plasticity=False)

@@ -296,3 +296,30 @@ def test_autotune_picks_a_candidate_and_leaves_state_untouched():
     ref = sc.make_solver(chunk=512)
     ref.step(2e-3)
     assert np.abs(s.particle_info()['position'] - ref.particle_info()['position']).max() < 1e-5
+
+
+def test_adaptive_dt_frames_match_oracle_with_the_same_steps():
+    """use_adaptive_dt=True (engine/mpm_solver.py:756-766): each substep's dt
+    is min(dt, 0.9 dx / (max grid |v| + 1e-6), time left), the frame's dts
+    add up to frame_dt, and the oracle run with the same dts lands on the
+    same positions."""
+    sc = scenes.smoke_scene()
+    sc.v[:] = np.float32([0.0, -6.0, 0.0])  # fast enough for the CFL bound to act
+    s = sc.make_solver(use_adaptive_dt=True)
+    frame_dt = 4e-3
+    s.step(frame_dt)
+    first = list(s.last_frame_dts)
+    s.step(frame_dt)
+    dts = s.last_frame_dts
+    assert abs(sum(dts) - frame_dt) < 1e-12
+    default = frame_dt / (int(frame_dt / s.default_dt) + 1)
+    assert min(dts) < default  # the CFL bound shortened some substeps
+    assert all(b <= a + 1e-15 for a, b in zip(dts, dts[1:-1]))  # dt never grows inside a frame
+    # oracle: the same two frames substep by substep
+    cfg = oracle_config(sc)
+    R = O.Runner(cfg, O.Particles.seeded(sc.x, sc.material, v=sc.v))
+    for dt in first + dts:
+        R.run(dt, 1)
+    g = s.full_state()['x'].cpu().numpy().astype(np.float64)
+    err = np.linalg.norm(g - R.P.x) / np.linalg.norm(R.P.x)
+    assert err < 1e-4, err

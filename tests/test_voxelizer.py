@@ -37,3 +37,33 @@ def test_padding_columns_stay_empty():
     res, dx = V.grid_res((16, 16, 16)), 1 / 32
     vox = V.voxelize(scenes.box_mesh((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), res, dx, padding=3)
     assert vox[:3].sum() == 0 and vox[-3:].sum() == 0 and vox[:, :3].sum() == 0 and vox[:, :, :3].sum() == 0
+
+
+def _write_ply(fn, verts, faces, fmt):
+    head = [f"ply", f"format {fmt} 1.0", "comment test", f"element vertex {len(verts)}", "property float x",
+            "property float y", "property float z", f"element face {len(faces)}",
+            "property list uchar int vertex_indices", "end_header"]
+    with open(fn, "wb") as f:
+        f.write(("\n".join(head) + "\n").encode())
+        if fmt == "ascii":
+            for v in verts:
+                f.write(f"{v[0]} {v[1]} {v[2]}\n".encode())
+            for fc in faces:
+                f.write(("3 " + " ".join(map(str, fc)) + "\n").encode())
+        else:
+            f.write(np.asarray(verts, "<f4").tobytes())
+            for fc in faces:
+                f.write(np.uint8(3).tobytes() + np.asarray(fc, "<i4").tobytes())
+
+
+def test_load_mesh_ascii_and_binary(tmp_path):
+    from taichi_elements_gb300.mesh_io import load_mesh
+    box = scenes.box_mesh((0.1, 0.2, 0.3), (0.4, 0.5, 0.6)).reshape(-1, 3)
+    verts, inv = np.unique(box, axis=0, return_inverse=True)
+    faces = inv.reshape(-1, 3)
+    for fmt in ("ascii", "binary_little_endian"):
+        fn = str(tmp_path / f"m_{fmt}.ply")
+        _write_ply(fn, verts, faces, fmt)
+        tri = load_mesh(fn, scale=2.0, offset=(1.0, 0.0, -1.0))
+        want = box.reshape(-1, 9).astype(np.float64) * 2.0 + np.tile([1.0, 0.0, -1.0], 3)
+        np.testing.assert_allclose(tri, want, rtol=1e-6, atol=1e-6)

@@ -607,6 +607,8 @@ class MPMSolver:
         self._cur = 1 - self._cur
 
     def _prepare(self, frame_dt: float = 0.0):
+        if self.n_particles == 0 and self._cap == 0:
+            return  # nothing to step and no buffers yet (the reference steps empty solvers)
         self._ensure_workspace()
         self._rebin()
         self._check_window_covers_particles(frame_dt)

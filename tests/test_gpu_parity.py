@@ -323,3 +323,52 @@ def test_adaptive_dt_frames_match_oracle_with_the_same_steps():
     g = s.full_state()['x'].cpu().numpy().astype(np.float64)
     err = np.linalg.norm(g - R.P.x) / np.linalg.norm(R.P.x)
     assert err < 1e-4, err
+
+
+def test_empty_cleared_and_refilled_solver():
+    s = MPMSolver((16, 16, 16))
+    s.step(1e-3)  # no particles: time advances, nothing launches
+    assert s.t > 0 and s.n_particles == 0
+    s.add_cube((0.3, 0.3, 0.3), (0.2, 0.2, 0.2), s.material_water)
+    n1 = s.n_particles
+    s.step(1e-3)
+    s.clear_particles()
+    assert s.n_particles == 0
+    s.step(1e-3)
+    s.add_cube((0.4, 0.4, 0.4), (0.1, 0.1, 0.1), s.material_elastic)
+    s.step(1e-3)
+    info = s.particle_info()
+    assert 0 < s.n_particles < n1 and np.isfinite(info['position']).all()
+    assert (info['material'] == s.material_elastic).all()
+
+
+def test_unbounded_trajectory_leaving_the_box_matches_oracle():
+    s = MPMSolver((16, 16, 16), unbounded=True)
+    s.add_cube((0.8, 0.4, 0.4), (0.1, 0.1, 0.1), s.material_elastic, velocity=(4.0, 0.0, 0.0))
+    x0 = s.particle_info()['position']
+    cfg = oracle_config(s)
+    lo = np.array([-16, -64, -16], np.int32)  # nodes; the particles travel +x and fall
+    win = O.Window(lo, np.array([96, 96, 64], np.int32))
+    R = O.Runner(cfg, O.Particles.seeded(x0, s.material_elastic, v=np.float32([4.0, 0.0, 0.0])), win=win)
+    dt = s.default_dt
+    for _ in range(60):
+        s.substep(dt)
+    R.run(dt, 60)
+    g = s.full_state()['x'].cpu().numpy().astype(np.float64)
+    assert g[:, 0].min() > 1.0  # left the nominal box
+    assert np.linalg.norm(g - R.P.x) / np.linalg.norm(R.P.x) < 1e-4
+
+
+def test_sticky_sphere_and_slip_plane_trajectory():
+    sc = scenes.smoke_scene()
+    sc.postprocess = [dict(kind=1, surface=0, point=(0.45, 0.3, 0.45), radius=0.1),
+                      dict(kind=0, surface=1, point=(0.5, 0.1, 0.5), normal=(0.0, 1.0, 0.2), friction=0.0)]
+    s = sc.make_solver()
+    cfg = oracle_config(sc)
+    R = O.Runner(cfg, O.Particles.seeded(sc.x, sc.material, v=sc.v))
+    dt = sc.default_dt
+    R.run(dt, 80)
+    for _ in range(80):
+        s.substep(dt)
+    g = s.full_state()['x'].cpu().numpy().astype(np.float64)
+    assert np.linalg.norm(g - R.P.x) / np.linalg.norm(R.P.x) < 1e-3

@@ -192,7 +192,7 @@ class BatchedMPM:
             a, b = int(self.offsets[i]), int(self.offsets[i + 1])
             s[ROW_X:ROW_X + 3, a:b] = torch.from_numpy(sc.x).t().to(self.device)
             s[ROW_V:ROW_V + 3, a:b] = torch.from_numpy(sc.v).t().to(self.device)
-            mat = torch.from_numpy(sc.material).to(self.device)
+            mat = torch.as_tensor(np.array(sc.material, dtype=np.int32)).to(self.device)
             si[ROW_MAT, a:b] = mat | (i << 8)
             s[ROW_JP, a:b] = torch.where(mat == 3, 0.0, 1.0)
         s[ROW_C:ROW_C + 9, :self.n_particles] = 0.0

@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define MPM_ABI_VERSION 3
+#define MPM_ABI_VERSION 4
 #define MPM_NROWS 28
 #define MPM_MAX_COLLIDERS 16 /* post-process records, box included */
 
@@ -80,12 +80,18 @@ typedef struct MpmParams {
   int32_t win_nb[3]; /* grid window extent in 4^3 blocks */
   int32_t has_Ep;    /* per-particle Young's modulus in pstate row 27 */
   int32_t chunk;     /* particles per P2G/G2P work item (multiple of 32) */
+  int32_t plasticity; /* support_plasticity (mpm_solver.py:62): 0 = no Jp
+                       * updates, h = 1, water restarts from F = I and sand
+                       * carries no stress */
   float dx, inv_dx, p_vol, p_mass;
   float mu0, la0, nu, alpha; /* Lame parameters, Poisson ratio, sand alpha */
   float water_density;
   float gravity[3];
   float stress_k; /* p_vol * 4 * inv_dx^2            (mpm_solver.py:569) */
   float sand_k;   /* (3 la0 + 2 mu0) / (2 mu0)        (mpm_solver.py:335-337) */
+  float v_clamp_k; /* dx * g2p2g_allowed_cfl when the fused G2P2G mode clamps
+                    * grid velocities to +-v_clamp_k / dt per component after
+                    * gravity (mpm_solver.py:589-598); 0 = no clamp */
   /* Batched mode only (zero otherwise).  Scenes live side by side in one
    * grid window, scene s in slot (s % slots[0], s / slots[0] % slots[1],
    * s / (slots[0]*slots[1])) of slot_nb blocks per axis.  Each scene's row of

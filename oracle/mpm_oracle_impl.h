@@ -56,6 +56,8 @@ typedef struct {
   REAL stress_scale_k; /* p_vol * 4 * inv_dx^2 */
   REAL sand_k;         /* (3 la0 + 2 mu0) / (2 mu0) */
   REAL nu;
+  int plasticity; /* support_plasticity (engine/mpm_solver.py:62) */
+  REAL v_clamp_k; /* dx * g2p2g_allowed_cfl, or 0 (no grid velocity clamp) */
 } FN(Consts);
 
 static void FN(make_consts)(const double *pd, FN(Consts) * c) {
@@ -74,6 +76,8 @@ static void FN(make_consts)(const double *pd, FN(Consts) * c) {
   c->stress_scale_k = (REAL)pd[11];
   c->sand_k = (REAL)pd[12];
   c->nu = (REAL)pd[13];
+  c->plasticity = pd[14] != 0.0;
+  c->v_clamp_k = (REAL)pd[15];
 }
 
 /* ---------------------------------------------------------------- SVD --- */
@@ -256,7 +260,11 @@ static void FN(sand_projection)(REAL sig[3], REAL *Jp, const FN(Consts) * k, REA
  * in place and returns the scatter inputs (mass, momentum m*v, affine). */
 /* fused != 0: the constitutive update of the G2P2G substep (:410-476):
  * no water F reset (:508-511), h = exp(10 (1 - Jp)) for every material,
- * water keeps Jp, mass = p_mass for every material. */
+ * water keeps Jp, mass = p_mass for every material.
+ * k->plasticity == 0 (support_plasticity=False): the reference has no Jp
+ * field; water restarts from F = I (:508-511), h = 1 (:516-518, :419-421),
+ * Jp is never updated (:533-534, :541-542) and sand has neither the return
+ * map nor a stress (:553-566). */
 static void FN(p2g_particle)(const FN(Consts) * k, REAL dt, int mat, REAL Ep,
                              REAL *F9, REAL *Jp, const REAL *C9, REAL *mass_out,
                              REAL affine[3][3], int fused) {
@@ -274,13 +282,13 @@ static void FN(p2g_particle)(const FN(Consts) * k, REAL dt, int mat, REAL Ep,
   if (!fused && mat == 0) { /* :508-511 */
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) F[i][j] = (REAL)(i == j);
-    F[0][0] = *Jp;
+    if (k->plasticity) F[0][0] = *Jp;
   }
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) G[i][j] = (REAL)(i == j) + dt * C[i][j];
   FN(matmul3)(G, F, Fn); /* :513 */
   REAL h = 1;
-  if (fused || mat != 0) h = EXP((REAL)10 * ((REAL)1 - *Jp)); /* :516-518, :427-429 */
+  if (k->plasticity && (fused || mat != 0)) h = EXP((REAL)10 * ((REAL)1 - *Jp)); /* :516-518, :427-429 */
   if (mat == 1) h = (REAL)0.3;                         /* :519-521 */
   REAL mu = mu0 * h, la = la0 * h;
   if (mat == 0) mu = 0;
@@ -300,7 +308,7 @@ static void FN(p2g_particle)(const FN(Consts) * k, REAL dt, int mat, REAL Ep,
         if (ns < (REAL)(1 - 2.5e-2)) ns = (REAL)(1 - 2.5e-2);
         if (ns > (REAL)(1 + 4.5e-3)) ns = (REAL)(1 + 4.5e-3);
       }
-      *Jp *= sg[d] / ns;
+      if (k->plasticity) *Jp *= sg[d] / ns;
       sg[d] = ns;
       J *= ns;
     }
@@ -310,7 +318,7 @@ static void FN(p2g_particle)(const FN(Consts) * k, REAL dt, int mat, REAL Ep,
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) Fn[i][j] = (REAL)(i == j);
     Fn[0][0] = J;
-    if (!fused) *Jp = J;
+    if (!fused && k->plasticity) *Jp = J;
   } else if (mat == 2) { /* :543-545 */
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j)
@@ -327,6 +335,9 @@ static void FN(p2g_particle)(const FN(Consts) * k, REAL dt, int mat, REAL Ep,
         REAL acc = D[i][0] * Fn[j][0] + D[i][1] * Fn[j][1] + D[i][2] * Fn[j][2];
         stress[i][j] = (REAL)2 * mu * acc + (i == j ? la * J * (J - (REAL)1) : (REAL)0);
       }
+  } else if (!k->plasticity) { /* sand without plasticity: zero stress, F kept */
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) stress[i][j] = 0;
   } else { /* :552-566 */
     FN(sand_projection)(sg, Jp, k, mu0, la0);
     for (int i = 0; i < 3; ++i)
@@ -405,8 +416,8 @@ static int FN(scatter_particle)(const FN(Window) * w, const REAL *xp, const REAL
   return 0;
 }
 
-/* Grid update for one node: engine/mpm_solver.py:586-598 (normalisation and
- * gravity), then the grid_postprocess list in order (:794-795): bounding box
+/* Grid update for one node: engine/mpm_solver.py:586-598 (normalisation,
+ * gravity and the fused mode's velocity clamp), then the grid_postprocess list in order (:794-795): bounding box
  * (:600-616, kind 2), sphere (:618-642, kind 1) and surface (:647-687,
  * kind 0) colliders.  coll: 12 doubles per record, see mpm_oracle.c. */
 static void FN(grid_node)(int gi, int gj, int gk, REAL m, REAL *v, REAL dt, const FN(Consts) * k,
@@ -416,6 +427,10 @@ static void FN(grid_node)(int gi, int gj, int gk, REAL m, REAL *v, REAL dt, cons
     REAL inv = (REAL)1 / m;
     for (int d = 0; d < 3; ++d) v[d] = inv * v[d];
     for (int d = 0; d < 3; ++d) v[d] += dt * k->gravity[d];
+  }
+  if (k->v_clamp_k > (REAL)0) { /* fused G2P2G mode, :589 and :594-598 */
+    REAL va = k->v_clamp_k / dt;
+    for (int d = 0; d < 3; ++d) v[d] = v[d] < -va ? -va : (v[d] > va ? va : v[d]);
   }
   int I[3] = {gi, gj, gk};
   (void)unbounded;

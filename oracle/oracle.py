@@ -19,6 +19,7 @@ F = I) and by agreement of the two restatements.
 from __future__ import annotations
 
 import ctypes
+import dataclasses
 import math
 import os
 import subprocess
@@ -84,6 +85,9 @@ class Config:
     unbounded: bool = False
     water_density: float = 1.0
     gravity: tuple = (0.0, -9.8, 0.0)
+    support_plasticity: bool = True
+    # fused G2P2G mode: grid velocities clamped to +-cfl * dx / dt (0 = off)
+    v_clamp_cfl: float = 0.0
     # grid_postprocess list; the bounding box first, as the constructor adds it
     postprocess: list = field(default_factory=lambda: [dict(kind=KIND_BOX, surface=0)])
 
@@ -110,7 +114,8 @@ class Config:
         return np.array([
             self.dx, self.inv_dx, self.p_vol, self.p_mass, self.mu_0, self.lambda_0, self.alpha, self.water_density,
             self.gravity[0], self.gravity[1], self.gravity[2], self.p_vol * 4 * self.inv_dx**2,
-            (3 * self.lambda_0 + 2 * self.mu_0) / (2 * self.mu_0), self.nu
+            (3 * self.lambda_0 + 2 * self.mu_0) / (2 * self.mu_0), self.nu, float(bool(self.support_plasticity)),
+            self.dx * self.v_clamp_cfl
         ], dtype=np.float64)
 
     def coll(self) -> np.ndarray:
@@ -331,9 +336,13 @@ class Runner:
 class G2P2GRunner:
     """The fused G2P2G mode (engine/mpm_solver.py:363-485, :773-787): the
     grid velocities persist between substeps; particles added since the last
-    substep (index >= last_final) skip the gather.  C is not carried."""
+    substep (index >= last_final) skip the gather.  C is not carried.
+    The grid update clamps velocities to +-v_clamp_cfl * dx / dt per
+    component (v_clamp_g2p2g=True and g2p2g_allowed_cfl=0.9 by default,
+    :589-598); v_clamp_cfl=0 turns the clamp off."""
 
-    def __init__(self, cfg: Config, P: Particles, win: Window):
+    def __init__(self, cfg: Config, P: Particles, win: Window, v_clamp_cfl: float = 0.9):
+        cfg = dataclasses.replace(cfg, v_clamp_cfl=v_clamp_cfl)
         self.cfg, self.P, self.win = cfg, P, win
         self.gv = np.zeros(win.nnodes * 3, P.x.dtype)
         self.last_final = 0
@@ -388,15 +397,16 @@ def np_substep(cfg: Config, P: Particles, dt: float):
     I3 = np.eye(3)
     Fw = F.copy()
     water = mat == MAT_WATER
+    plast = bool(cfg.support_plasticity)
     Fw[water] = I3
-    Fw[water, 0, 0] = Jp[water]
+    Fw[water, 0, 0] = Jp[water] if plast else 1.0  # :508-511
     Fn = (I3 + dt * C) @ Fw
     mu0 = np.full(n, cfg.mu_0) if P.E is None else P.E / (2 * (1 + cfg.nu))
     la0 = np.full(n, cfg.lambda_0) if P.E is None else P.E * cfg.nu / ((1 + cfg.nu) * (1 - 2 * cfg.nu))
     if P.E is not None:
         mu0 = np.where(P.E > 0, mu0, cfg.mu_0)
         la0 = np.where(P.E > 0, la0, cfg.lambda_0)
-    h = np.where(mat != MAT_WATER, np.exp(10 * (1 - Jp)), 1.0)
+    h = np.where((mat != MAT_WATER) & plast, np.exp(10 * (1 - Jp)), 1.0)
     h = np.where(mat == MAT_ELASTIC, 0.3, h)
     mu = np.where(water, 0.0, mu0 * h)
     la = la0 * h
@@ -417,7 +427,10 @@ def np_substep(cfg: Config, P: Particles, dt: float):
     R = U @ np.swapaxes(V, -1, -2)
     stress = 2 * mu[:, None, None] * (Fnew - R) @ np.swapaxes(Fnew, -1, -2) + \
         (la * J * (J - 1))[:, None, None] * I3
-    if sand.any():
+    if not plast:  # no Jp field; sand carries no stress (:553-566 skipped)
+        Jp_new = Jp.copy()
+        stress[sand] = 0.0
+    elif sand.any():
         s_ = sig[sand]
         eps = np.log(np.maximum(np.abs(s_), 1e-4))
         tr = eps.sum(1) + Jp[sand]

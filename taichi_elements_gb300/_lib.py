@@ -12,7 +12,7 @@ from pathlib import Path
 
 from . import build as _build
 
-ABI_VERSION = 3
+ABI_VERSION = 4
 NROWS = 28
 MAX_COLLIDERS = 16
 
@@ -53,6 +53,7 @@ class MpmParams(ctypes.Structure):
         ("win_nb", ctypes.c_int32 * 3),
         ("has_Ep", ctypes.c_int32),
         ("chunk", ctypes.c_int32),
+        ("plasticity", ctypes.c_int32),
         ("dx", ctypes.c_float),
         ("inv_dx", ctypes.c_float),
         ("p_vol", ctypes.c_float),
@@ -65,6 +66,7 @@ class MpmParams(ctypes.Structure):
         ("gravity", ctypes.c_float * 3),
         ("stress_k", ctypes.c_float),
         ("sand_k", ctypes.c_float),
+        ("v_clamp_k", ctypes.c_float),
         ("n_scenes", ctypes.c_int32),
         ("slot_nb", ctypes.c_int32 * 3),
         ("slots", ctypes.c_int32 * 3),

@@ -137,6 +137,7 @@ class BatchedMPM:
             p.slots[d] = self.slots[d]
             p.res[d] = 1
         p.chunk = self.chunk
+        p.plasticity = 1
         p.n_scenes = len(self.scenes)
         return p
 

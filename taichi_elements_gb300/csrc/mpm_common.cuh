@@ -184,6 +184,10 @@ struct P2GOut {
 // fused G2P2G substep (:419-476): no water F reset before the update
 // (:508-511), hardening h = exp(10 (1 - Jp)) for every material, water keeps
 // its Jp (:537-542 sets only F) and the mass is p_mass for every material.
+// P.plasticity == 0 is support_plasticity=False: the reference then has no Jp
+// field, so water restarts from F = I (:508-511), h = 1 (:516-518), Jp is
+// never updated (:533-534, :541-542) and sand carries no stress and keeps
+// (I + dt C) F (:553-566 are skipped).
 template <bool FUSED = false>
 __device__ __forceinline__ P2GOut constitutive(const MpmParams &P, float dt, int mat, float Ep,
                                                float (&F)[3][3], float &Jp, const float (&C)[3][3]) {
@@ -197,7 +201,7 @@ __device__ __forceinline__ P2GOut constitutive(const MpmParams &P, float dt, int
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int j = 0; j < 3; ++j) F[i][j] = (i == j) ? 1.0f : 0.0f;
-    F[0][0] = Jp;
+    F[0][0] = P.plasticity ? Jp : 1.0f;
   }
   float Fn[3][3];  // (I + dt C) F, :513
 #pragma unroll
@@ -211,7 +215,7 @@ __device__ __forceinline__ P2GOut constitutive(const MpmParams &P, float dt, int
       Fn[i][j] = acc;
     }
   float h = 1.0f;
-  if (FUSED || mat != 0) h = expf(10.0f * (1.0f - Jp));  // :516-518 (:427-429)
+  if (P.plasticity && (FUSED || mat != 0)) h = expf(10.0f * (1.0f - Jp));  // :516-518 (:427-429)
   if (mat == 1) h = 0.3f;                       // :519-521
   float mu = mu0 * h;
   const float la = la0 * h;
@@ -232,7 +236,12 @@ __device__ __forceinline__ P2GOut constitutive(const MpmParams &P, float dt, int
         stress[i][j] = (i == j) ? la * J * (J - 1.0f) : 0.0f;
       }
     Fn[0][0] = J;
-    if (!FUSED) Jp = J;
+    if (!FUSED && P.plasticity) Jp = J;
+  } else if (mat == 3 && !P.plasticity) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) stress[i][j] = 0.0f;
   } else {
     if (mat == 1 || mat == 4 || mat == 2) {
       // Elastic and stationary particles never clamp sigma (:527-536), and a
@@ -287,7 +296,7 @@ __device__ __forceinline__ P2GOut constitutive(const MpmParams &P, float dt, int
       for (int d = 0; d < 3; ++d) {
         float ns = sg[d];
         if (mat == 2) ns = fminf(fmaxf(ns, 1.0f - 2.5e-2f), 1.0f + 4.5e-3f);  // :530-532
-        Jp *= sg[d] / ns;                                                         // :534
+        if (P.plasticity) Jp *= sg[d] / ns;                                       // :534
         sg[d] = ns;
         J *= ns;
       }
@@ -433,8 +442,9 @@ __device__ __forceinline__ void postprocess_op(const MpmParams &P, const MpmColl
   }
 }
 
-// Grid node update, engine/mpm_solver.py:586-598 (momentum to velocity and
-// gravity) followed by the post-process list in order.
+// Grid node update, engine/mpm_solver.py:586-598 (momentum to velocity,
+// gravity and, in the fused G2P2G mode, the per-component velocity clamp to
+// dx * cfl / dt) followed by the post-process list in order.
 __device__ __forceinline__ float3 grid_node_update(const MpmParams &P, const int (&I)[3], float m,
                                                    float3 mv, float dt) {
   float v[3] = {mv.x, mv.y, mv.z};
@@ -442,6 +452,11 @@ __device__ __forceinline__ float3 grid_node_update(const MpmParams &P, const int
     const float inv = 1.0f / m;
 #pragma unroll
     for (int d = 0; d < 3; ++d) v[d] = inv * v[d] + dt * P.gravity[d];
+  }
+  if (P.v_clamp_k > 0.0f) {  // :594-598
+    const float va = P.v_clamp_k / dt;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) v[d] = fminf(fmaxf(v[d], -va), va);
   }
   for (int c = 0; c < P.n_colliders; ++c) postprocess_op(P, P.colliders[c], I, v);
   return make_float3(v[0], v[1], v[2]);

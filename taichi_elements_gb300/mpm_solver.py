@@ -100,8 +100,6 @@ class MPMSolver:
             raise NotImplementedError("the GB300 engine implements the 3-D solver only")
         if quant:
             raise NotImplementedError("quantised particle storage (quant=True) is not implemented")
-        if not support_plasticity:
-            raise NotImplementedError("support_plasticity=False is not implemented")
 
         self.device = torch.device(device if device is not None else "cuda")
         if self.device.type != "cuda" or not torch.cuda.is_available():
@@ -217,6 +215,7 @@ class MPMSolver:
         p.grid_size = self.grid_size
         p.has_Ep = int(self.per_particle_E)
         p.chunk = self.chunk
+        p.plasticity = int(bool(self.support_plasticity))
         p.dx = self.dx
         p.inv_dx = self.inv_dx
         p.p_vol = self.p_vol
@@ -230,6 +229,8 @@ class MPMSolver:
             p.gravity[d] = self.gravity[d]
         p.stress_k = self.p_vol * 4 * self.inv_dx**2
         p.sand_k = (self.dim * self.lambda_0 + 2 * self.mu_0) / (2 * self.mu_0)
+        if self.use_g2p2g and self.v_clamp_g2p2g and self.g2p2g_allowed_cfl > 0:
+            p.v_clamp_k = self.dx * self.g2p2g_allowed_cfl  # :589, :594-598
         if len(self.grid_postprocess) > _lib.MAX_COLLIDERS:
             raise ValueError(f"at most {_lib.MAX_COLLIDERS} grid post-process entries are supported")
         p.n_colliders = len(self.grid_postprocess)

@@ -55,7 +55,7 @@ def _c_layout():
 #define P(T, f) printf(#T "." #f " %zu\n", offsetof(T, f))
 int main(void) {
   printf("MpmParams %zu\nMpmCollider %zu\nMpmViews %zu\n", sizeof(MpmParams), sizeof(MpmCollider), sizeof(MpmViews));
-  P(MpmParams, win_lo); P(MpmParams, chunk); P(MpmParams, dx); P(MpmParams, gravity); P(MpmParams, stress_k);
+  P(MpmParams, win_lo); P(MpmParams, chunk); P(MpmParams, plasticity); P(MpmParams, dx); P(MpmParams, gravity); P(MpmParams, stress_k);
   P(MpmParams, sand_k); P(MpmParams, colliders); P(MpmCollider, normal); P(MpmCollider, friction);
   P(MpmViews, grid_vel);
   return 0;
@@ -77,6 +77,7 @@ def test_ctypes_struct_layout_matches_c():
     assert int(lay["MpmViews"]) == ctypes.sizeof(_lib.MpmViews)
     for key, (cls, field) in {
             "MpmParams.win_lo": (_lib.MpmParams, "win_lo"), "MpmParams.chunk": (_lib.MpmParams, "chunk"),
+            "MpmParams.plasticity": (_lib.MpmParams, "plasticity"),
             "MpmParams.dx": (_lib.MpmParams, "dx"), "MpmParams.gravity": (_lib.MpmParams, "gravity"),
             "MpmParams.stress_k": (_lib.MpmParams, "stress_k"), "MpmParams.sand_k": (_lib.MpmParams, "sand_k"),
             "MpmParams.colliders": (_lib.MpmParams, "colliders"),
@@ -120,5 +121,3 @@ def test_unsupported_flags_raise():
         MPMSolver((16, 16))
     with pytest.raises(NotImplementedError):
         MPMSolver((16, 16, 16), quant=True)
-    with pytest.raises(NotImplementedError):
-        MPMSolver((16, 16, 16), support_plasticity=False)

@@ -105,3 +105,38 @@ def test_g2p2g_frames_and_particles_added_between_frames():
     assert rel_inf(g['v'], R.P.v, max(np.abs(R.P.v).max(), 1e-3)) < 1e-4
     new = np.arange(R.last_final, P.n)
     assert np.allclose(g['v'][new], R.P.v[new], atol=1e-5)
+
+
+@pytest.mark.parametrize("v_clamp", [True, False])
+def test_g2p2g_grid_velocity_clamp(v_clamp):
+    """A cube launched faster than the CFL bound: with v_clamp_g2p2g=True
+    (the default) the grid velocities are clamped to +-0.9 dx / dt per
+    component after gravity (engine/mpm_solver.py:589-598), so the gathered
+    particle velocities stay inside it; with v_clamp_g2p2g=False they do not.
+    Both match the oracle run with the same setting."""
+    rng = np.random.default_rng(11)
+    res = (64, 64, 64)
+    dt = 2e-2 / 64
+    va = 0.9 * (1 / 64) / dt
+    n = 8000
+    x = (0.4 + 0.15 * rng.random((n, 3))).astype(np.float32)
+    v = np.broadcast_to(np.array([1.4 * va, -1.2 * va, 0.5 * va], np.float32), (n, 3)).copy()
+    sc = scenes.Scene("fast_cube_64", res, x, v, np.full(n, scenes.WATER, np.int32), 4)
+    s = sc.make_solver(use_g2p2g=True, v_clamp_g2p2g=v_clamp)
+    cfg = oracle_config(sc)
+    P64 = O.Particles.seeded(sc.x, sc.material, v=sc.v)
+    win = O.Window.covering(P64.x, cfg.inv_dx, margin=24)
+    cfl = 0.9 if v_clamp else 0.0
+    R64 = O.G2P2GRunner(cfg, P64, win, v_clamp_cfl=cfl)
+    R32 = O.G2P2GRunner(cfg, P64.astype(np.float32), win, v_clamp_cfl=cfl)
+    for _ in range(4):
+        s.substep(dt)
+        R64.step(dt)
+        R32.step(dt)
+    for k, (g, f32) in errors(s, R64, R32, win).items():
+        assert g <= max(TOL[k], 4 * f32), f"{k}: gpu {g:.3g} vs f32-oracle {f32:.3g}"
+    vmax = np.abs(gpu_particles(s)['v']).max(0)
+    if v_clamp:
+        assert np.all(vmax <= va * (1 + 1e-6)), vmax
+    else:
+        assert vmax[0] > 1.3 * va, vmax

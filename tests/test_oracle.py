@@ -97,6 +97,61 @@ def test_c_oracle_matches_numpy_restatement_per_particle_E():
         assert rel(getattr(P, f), getattr(out, f)) < 1e-10, f
 
 
+def test_c_oracle_matches_numpy_restatement_without_plasticity():
+    """support_plasticity=False (engine/mpm_solver.py:62): both restatements
+    agree, Jp never changes, sand keeps (I + dt C) F and water restarts from
+    F = I (its F[0,0] is det(I + dt C))."""
+    rng = np.random.default_rng(5)
+    cfg = O.Config(res=(32, 32, 32), support_plasticity=False)
+    n = 600
+    x = 0.3 + 0.4 * rng.random((n, 3))
+    mat = rng.integers(0, 5, n)
+    P = O.Particles.seeded(x, mat, v=rng.uniform(-1, 1, (n, 3)))
+    P.F = P.F + 0.02 * rng.standard_normal((n, 3, 3))
+    P.C = 5.0 * rng.standard_normal((n, 3, 3))
+    P.Jp = P.Jp * rng.uniform(0.9, 1.1, n)
+    P0 = P.copy()
+    Pn = P.copy()
+    dt = 1e-4
+    out, _ = O.np_substep(cfg, Pn, dt)
+    O.substep(cfg, P, dt)
+    for f in ("x", "v", "F", "Jp"):
+        assert rel(getattr(P, f), getattr(out, f)) < 1e-10, f
+    np.testing.assert_array_equal(P.Jp, P0.Jp)
+    G = np.eye(3) + dt * P0.C
+    sand = mat == O.MAT_SAND
+    np.testing.assert_allclose(P.F[sand], (G @ P0.F)[sand], rtol=0, atol=1e-14)
+    water = mat == O.MAT_WATER
+    np.testing.assert_allclose(P.F[water, 0, 0], np.linalg.det(G[water]), rtol=1e-12)
+    # with plasticity the same state takes different Jp and sand F
+    Pp = P0.copy()
+    O.substep(O.Config(res=(32, 32, 32)), Pp, dt)
+    assert not np.array_equal(Pp.Jp, P0.Jp)
+
+
+def test_g2p2g_oracle_clamps_grid_velocity():
+    """The fused mode clamps grid velocities to +-cfl * dx / dt per component
+    after gravity (engine/mpm_solver.py:589-598); the gathered particle
+    velocities then stay inside the bound."""
+    rng = np.random.default_rng(6)
+    cfg = O.Config(res=(32, 32, 32))
+    n = 2000
+    x = 0.4 + 0.2 * rng.random((n, 3))
+    dt = cfg.default_dt
+    va = 0.9 * cfg.dx / dt
+    v0 = np.array([1.4 * va, -1.2 * va, 0.5 * va])
+    out = {}
+    for cfl in (0.9, 0.0):
+        P = O.Particles.seeded(x, O.MAT_WATER, v=v0)
+        win = O.Window.covering(P.x, cfg.inv_dx, margin=24)
+        R = O.G2P2GRunner(cfg, P, win, v_clamp_cfl=cfl)
+        for _ in range(3):
+            R.step(dt)
+        out[cfl] = np.abs(R.P.v).max(0)
+    assert np.all(out[0.9] <= va * (1 + 1e-12))
+    assert out[0.0][0] > 1.3 * va
+
+
 # --------------------------------------------------------- known answers --
 
 def test_single_particle_partition_of_unity():

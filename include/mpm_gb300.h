@@ -23,6 +23,15 @@
  *   27 per-particle Young's modulus (used only when MpmParams.has_Ep != 0).
  * The engine ping-pongs between two such buffers: a substep reads buffer
  * `cur` in any order and writes buffer `nxt` sorted by grid block.
+ *
+ * With MpmParams.quant != 0 (MPMSolver(quant=True), engine/mpm_solver.py
+ * :106-127 and :216-262) the buffers hold MPM_QROWS rows of 32-bit words:
+ *   rows 0-1 x as three signed 21-bit fixed-point values of scale 2^-19,
+ *   rows 2-3 v as a 7-bit shared exponent (bias 100) and three signed 19-bit
+ *   mantissas, rows 4-8 F as nine signed 16-bit fixed-point values of scale
+ *   4.1/2^15 two per word, the last word's high half holding the 16-bit
+ *   material, 9 Jp, 10 id, 11 Young's modulus, 12-20 C (float32).
+ * mpm_quant_pack / mpm_quant_unpack convert between the two layouts.
  */
 #ifndef MPM_GB300_H
 #define MPM_GB300_H
@@ -34,8 +43,9 @@
 extern "C" {
 #endif
 
-#define MPM_ABI_VERSION 4
+#define MPM_ABI_VERSION 5
 #define MPM_NROWS 28
+#define MPM_QROWS 21
 #define MPM_MAX_COLLIDERS 16 /* post-process records, box included */
 
 /* status bits (workspace status word) */
@@ -83,6 +93,8 @@ typedef struct MpmParams {
   int32_t plasticity; /* support_plasticity (mpm_solver.py:62): 0 = no Jp
                        * updates, h = 1, water restarts from F = I and sand
                        * carries no stress */
+  int32_t quant;      /* quant=True (mpm_solver.py:106-127, :216-262): pstate
+                       * holds the packed 21-row layout (MPM_QROWS) */
   float dx, inv_dx, p_vol, p_mass;
   float mu0, la0, nu, alpha; /* Lame parameters, Poisson ratio, sand alpha */
   float water_density;
@@ -259,6 +271,19 @@ int mpm_substep_noalloc(const MpmParams *p, int64_t cap, int64_t n, const float 
  * Replaces copy_dynamic_nd / copy_dynamic, engine/mpm_solver.py:1146-1191. */
 int mpm_gather_rows(const float *pstate, int64_t cap, int64_t n, int32_t row0, int32_t ncols,
                     float *out, void *stream);
+
+/* Packed particle storage (quant=True).  mpm_quant_pack encodes slots
+ * [begin, end) of a float32-layout buffer (MPM_NROWS rows of stride
+ * rows_cap) into the packed buffer (MPM_QROWS rows of stride cap), rounding
+ * to the nearest representable value (ties away from zero); positions
+ * outside [-2, 2) are clamped and OR MPM_STATUS_OUT_OF_GRID into *status
+ * (device int32, may be null), non-finite values MPM_STATUS_NONFINITE.
+ * mpm_quant_unpack decodes the same slots back into the float32 layout
+ * (rows 25 and 26 carry the material and id as int32 bits). */
+int mpm_quant_pack(const float *rows, int64_t rows_cap, int64_t begin, int64_t end, float *packed, int64_t cap,
+                   int32_t *status, void *stream);
+int mpm_quant_unpack(const float *packed, int64_t cap, int64_t begin, int64_t end, float *rows, int64_t rows_cap,
+                     void *stream);
 
 /* ---- Particle output (engine/particle_io.py:12-76, ParticleIO.write_particles)
  * The quantised frame format: per dimension, positions and velocities are

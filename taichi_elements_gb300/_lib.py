@@ -12,8 +12,9 @@ from pathlib import Path
 
 from . import build as _build
 
-ABI_VERSION = 4
+ABI_VERSION = 5
 NROWS = 28
+QROWS = 21  # packed rows of quant=True (MPM_QROWS)
 MAX_COLLIDERS = 16
 
 STATUS_OUT_OF_GRID = 1
@@ -54,6 +55,7 @@ class MpmParams(ctypes.Structure):
         ("has_Ep", ctypes.c_int32),
         ("chunk", ctypes.c_int32),
         ("plasticity", ctypes.c_int32),
+        ("quant", ctypes.c_int32),
         ("dx", ctypes.c_float),
         ("inv_dx", ctypes.c_float),
         ("p_vol", ctypes.c_float),
@@ -130,6 +132,8 @@ SIGNATURES = {
     "mpm_p2g_adj": [_P, _v, _i64, _i64, _v, _f, _v, _v, _v, _v, _i32, _v],
     "mpm_batch_substep": [_P, _v, _v, _i64, _i64, _v, _v, _v, _v],
     "mpm_gather_rows": [_v, _i64, _i64, _i32, _i32, _v, _v],
+    "mpm_quant_pack": [_v, _i64, _i64, _i64, _v, _i64, _v, _v],
+    "mpm_quant_unpack": [_v, _i64, _i64, _i64, _v, _i64, _v],
     "mpm_status_ptr": [_P, _v, _i64, ctypes.POINTER(ctypes.c_void_p)],
     "mpm_max_grid_velocity": [_P, _v, _i64, _v, _v],
     "mpm_views": [_P, _v, _i64, ctypes.POINTER(MpmViews)],

@@ -671,7 +671,7 @@ static int adj_dev_sms() {
 }
 
 static bool adj_params_ok(const MpmParams *p) {
-  if (!p || p->version != MPM_ABI_VERSION || p->chunk < 32 || (p->chunk & 31) != 0) return false;
+  if (!p || p->version != MPM_ABI_VERSION || p->quant || p->chunk < 32 || (p->chunk & 31) != 0) return false;
   for (int d = 0; d < 3; ++d)
     if (p->win_nb[d] <= 0 || (p->win_lo[d] & 3) != 0) return false;
   return p->n_colliders >= 0 && p->n_colliders <= MPM_MAX_COLLIDERS;

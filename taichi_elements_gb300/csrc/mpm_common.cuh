@@ -7,6 +7,7 @@
 #include <stdint.h>
 
 #include "mpm_gb300.h"
+#include "quant.cuh"
 #include "svd3.cuh"
 
 namespace mpm {
@@ -188,7 +189,12 @@ struct P2GOut {
 // field, so water restarts from F = I (:508-511), h = 1 (:516-518), Jp is
 // never updated (:533-534, :541-542) and sand carries no stress and keeps
 // (I + dt C) F (:553-566 are skipped).
-template <bool FUSED = false>
+// FUSED with Q (quant=True) follows the fused kernel's reads of the packed
+// field: (I + dt C) F is clamped to +-F_bound = 4 (:415-416) and rounded to
+// the 16-bit fixed-point grid before the SVD, and the F rebuilt for snow and
+// sand is rounded before the stress reads it (:446-447, :458-469).  The
+// unfused P2G keeps its local F for the stress and rounds only on store.
+template <bool FUSED = false, bool Q = false>
 __device__ __forceinline__ P2GOut constitutive(const MpmParams &P, float dt, int mat, float Ep,
                                                float (&F)[3][3], float &Jp, const float (&C)[3][3]) {
   float mu0 = P.mu0, la0 = P.la0;
@@ -214,6 +220,12 @@ __device__ __forceinline__ P2GOut constitutive(const MpmParams &P, float dt, int
       acc = fmaf(dt * C[i][2], F[2][j], acc);
       Fn[i][j] = acc;
     }
+  if (FUSED && Q) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) Fn[i][j] = q_fixed_F(fminf(fmaxf(Fn[i][j], -4.0f), 4.0f));
+  }
   float h = 1.0f;
   if (P.plasticity && (FUSED || mat != 0)) h = expf(10.0f * (1.0f - Jp));  // :516-518 (:427-429)
   if (mat == 1) h = 0.3f;                       // :519-521
@@ -304,8 +316,10 @@ __device__ __forceinline__ P2GOut constitutive(const MpmParams &P, float dt, int
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
-          for (int j = 0; j < 3; ++j)
+          for (int j = 0; j < 3; ++j) {
             Fn[i][j] = U[i][0] * sg[0] * V[j][0] + U[i][1] * sg[1] * V[j][1] + U[i][2] * sg[2] * V[j][2];
+            if (FUSED && Q) Fn[i][j] = q_fixed_F(Fn[i][j]);
+          }
       }
       // :549-551  stress = 2 mu (F - U V^T) F^T + la J (J-1) I
       float D[3][3];
@@ -346,8 +360,10 @@ __device__ __forceinline__ P2GOut constitutive(const MpmParams &P, float dt, int
 #pragma unroll
       for (int i = 0; i < 3; ++i)
 #pragma unroll
-        for (int j = 0; j < 3; ++j)
+        for (int j = 0; j < 3; ++j) {
           Fn[i][j] = U[i][0] * sg[0] * V[j][0] + U[i][1] * sg[1] * V[j][1] + U[i][2] * sg[2] * V[j][2];
+          if (FUSED && Q) Fn[i][j] = q_fixed_F(Fn[i][j]);
+        }
       float ls = 0.0f, cen[3];
 #pragma unroll
       for (int i = 0; i < 3; ++i) {

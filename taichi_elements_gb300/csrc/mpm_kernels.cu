@@ -100,14 +100,16 @@ __device__ __forceinline__ void bin_one(const MpmParams &P, const MpmParams *tab
   w.cellkey[i] = key;
 }
 
-template <bool BATCH>
+template <bool BATCH, bool Q>
 __global__ void k_bin_count(const MpmParams P, const MpmParams *tab, const Ws w, const float *__restrict__ ps,
                             int64_t cap, int64_t begin, int64_t end) {
   const int64_t i = begin + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t bad = 0;
   if (i < end) {
-    const int matword = BATCH ? __float_as_int(ps[kMat * cap + i]) : 0;
-    bin_one<BATCH>(P, tab, w, i, ps[kX * cap + i], ps[(kX + 1) * cap + i], ps[(kX + 2) * cap + i], matword, bad);
+    const int matword = BATCH ? ld_mat<Q>(ps, cap, i) : 0;
+    float x[3];
+    ld_x<Q>(ps, cap, i, x);
+    bin_one<BATCH>(P, tab, w, i, x[0], x[1], x[2], matword, bad);
   }
   set_status(w, bad);
 }
@@ -370,7 +372,7 @@ __device__ __forceinline__ float4 f4add(float4 a, float4 b) {
   return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
 }
 
-template <bool HAS_EP, bool BATCH>
+template <bool HAS_EP, bool BATCH, bool Q>
 __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_p2g(const MpmParams P, const MpmParams *tab, const Ws w,
                                                        const float *__restrict__ cur,
                                                        float *__restrict__ nxt, int64_t cap, float dt) {
@@ -403,39 +405,31 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_p2g(const Mpm
       float wt[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
       int lx = 0, ly = 0, lz = 0;
       if (active) {
-        const float *src = cur + i;
-        float *dst = nxt + j;
+        using R = PRows<Q>;
         float x[3], v[3], C[3][3], F[3][3];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) x[d] = src[(kX + d) * cap];
-        const int matword = __float_as_int(src[kMat * cap]);
+        ld_x<Q>(cur, cap, i, x);
+        const int matword = ld_mat<Q>(cur, cap, i);
         const int mat = matword & 0xFF;
         const MpmParams &S = scene_of_particle<BATCH>(P, tab, matword);
-        const float Ep = HAS_EP ? src[kEp * cap] : 0.0f;
+        const float Ep = HAS_EP ? cur[R::Ep * cap + i] : 0.0f;
         // carried fields go to the sorted position j right away
-#pragma unroll
-        for (int d = 0; d < 3; ++d) dst[(kX + d) * cap] = x[d];
-        dst[kMat * cap] = __int_as_float(matword);
-        dst[kId * cap] = src[kId * cap];
-        if (HAS_EP) dst[kEp * cap] = Ep;
+        cp_x<Q>(cur, i, nxt, j, cap);
+        nxt[R::Id * cap + j] = cur[R::Id * cap + i];
+        if (HAS_EP) nxt[R::Ep * cap + j] = Ep;
         const Base b = particle_base(S, x[0], x[1], x[2], bad);
+        ld_v<Q>(cur, cap, i, v);
+        ld_F<Q>(cur, cap, i, F);
 #pragma unroll
-        for (int d = 0; d < 3; ++d) v[d] = src[(kV + d) * cap];
-#pragma unroll
-        for (int a = 0; a < 9; ++a) {
-          C[a / 3][a % 3] = src[(kC + a) * cap];
-          F[a / 3][a % 3] = src[(kF + a) * cap];
-        }
-        float Jp = src[kJp * cap];
+        for (int a = 0; a < 9; ++a) C[a / 3][a % 3] = cur[(R::C + a) * cap + i];
+        float Jp = cur[R::Jp * cap + i];
         const P2GOut o = constitutive(S, BATCH ? S.dt : dt, mat, Ep, F, Jp, C);
-#pragma unroll
-        for (int a = 0; a < 9; ++a) dst[(kF + a) * cap] = F[a / 3][a % 3];
-        dst[kJp * cap] = Jp;
+        st_F_mat<Q>(nxt, cap, j, F, matword);
+        nxt[R::Jp * cap + j] = Jp;
         if (mat == 4) {  // stationary: G2P keeps v and C (:722)
 #pragma unroll
-          for (int d = 0; d < 3; ++d) dst[(kV + d) * cap] = v[d];
+          for (int r = 0; r < (Q ? 2 : 3); ++r) nxt[(R::V + r) * cap + j] = cur[(R::V + r) * cap + i];
 #pragma unroll
-          for (int a = 0; a < 9; ++a) dst[(kC + a) * cap] = C[a / 3][a % 3];
+          for (int a = 0; a < 9; ++a) nxt[(R::C + a) * cap + j] = C[a / 3][a % 3];
         }
         lx = b.b[0] - bx * 4;
         ly = b.b[1] - by * 4;
@@ -535,7 +529,7 @@ __global__ __launch_bounds__(256) void k_grid(const MpmParams P, const MpmParams
 
 // ---------------------------------------------------------------- G2P ----
 
-template <bool BATCH>
+template <bool BATCH, bool Q>
 __global__ __launch_bounds__(kG2PThreads, 8) void k_g2p(const MpmParams P, const MpmParams *tab, const Ws w,
                                                        float *__restrict__ st, int64_t cap, float dt,
                                                        float *maxv_out) {
@@ -560,9 +554,8 @@ __global__ __launch_bounds__(kG2PThreads, 8) void k_g2p(const MpmParams P, const
     __syncthreads();
     for (int j = start + threadIdx.x; j < end; j += blockDim.x) {
       float x[3];
-#pragma unroll
-      for (int d = 0; d < 3; ++d) x[d] = st[(kX + d) * cap + j];
-      const int matword = __float_as_int(st[kMat * cap + j]);
+      ld_x<Q>(st, cap, j, x);
+      const int matword = ld_mat<Q>(st, cap, j);
       const int mat = matword & 0xFF;
       const MpmParams &S = scene_of_particle<BATCH>(P, tab, matword);
       const float s4 = 4.0f * S.inv_dx;
@@ -615,19 +608,17 @@ __global__ __launch_bounds__(kG2PThreads, 8) void k_g2p(const MpmParams P, const
         nC[r][2] = s4 * fmaf(-nv[r], b.fx[2], sc[r]);
       }
       float vv[3];
-      if (mat != 4) {  // :722-724
+      if (mat != 4) {  // :722-724; the advection reads the stored (rounded, when packed) v
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          vv[d] = nv[d];
-          x[d] = x[d] + dts * nv[d];
-          st[(kV + d) * cap + j] = nv[d];
-          st[(kX + d) * cap + j] = x[d];
-        }
+        for (int d = 0; d < 3; ++d) vv[d] = nv[d];
+        st_v<Q>(st, cap, j, vv, bad);
 #pragma unroll
-        for (int a = 0; a < 9; ++a) st[(kC + a) * cap + j] = nC[a / 3][a % 3];
+        for (int d = 0; d < 3; ++d) x[d] = x[d] + dts * vv[d];
+        st_x<Q>(st, cap, j, x, bad);
+#pragma unroll
+        for (int a = 0; a < 9; ++a) st[(PRows<Q>::C + a) * cap + j] = nC[a / 3][a % 3];
       } else {
-#pragma unroll
-        for (int d = 0; d < 3; ++d) vv[d] = st[(kV + d) * cap + j];
+        ld_v<Q>(st, cap, j, vv);
       }
       vmax = fmaxf(vmax, fmaxf(fabsf(vv[0]), fmaxf(fabsf(vv[1]), fabsf(vv[2]))));
       bin_one<BATCH>(P, tab, w, j, x[0], x[1], x[2], matword, bad);  // next substep's build_pid
@@ -665,6 +656,7 @@ __global__ __launch_bounds__(kG2PThreads, 8) void k_g2p(const MpmParams P, const
 constexpr int kFusedTileW = 8;
 constexpr int kFusedTileN = kFusedTileW * kFusedTileW * kFusedTileW;
 
+template <bool Q>
 __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_g2p2g(const MpmParams P, const Ws w,
                                                                          const float *__restrict__ cur,
                                                                          float *__restrict__ nxt, int64_t cap,
@@ -708,21 +700,16 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_g2p2g(const M
       float wt[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
       int tx0 = 0, ty0 = 0, tz0 = 0, gb[3] = {0, 0, 0};
       if (active) {
-        const float *src = cur + i;
-        float *dst = nxt + j;
+        using R = PRows<Q>;
         float x[3], v[3], F[3][3];
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          x[d] = src[(kX + d) * cap];
-          v[d] = src[(kV + d) * cap];
-        }
-#pragma unroll
-        for (int a = 0; a < 9; ++a) F[a / 3][a % 3] = src[(kF + a) * cap];
-        float Jp = src[kJp * cap];
-        const int matword = __float_as_int(src[kMat * cap]);
+        ld_x<Q>(cur, cap, i, x);
+        ld_v<Q>(cur, cap, i, v);
+        ld_F<Q>(cur, cap, i, F);
+        float Jp = cur[R::Jp * cap + i];
+        const int matword = ld_mat<Q>(cur, cap, i);
         const int mat = matword & 0xFF;
-        const float idf = src[kId * cap];
-        const float Ep = P.has_Ep ? src[kEp * cap] : 0.0f;
+        const float idf = cur[R::Id * cap + i];
+        const float Ep = P.has_Ep ? cur[R::Ep * cap + i] : 0.0f;
         // ---- G2P at x (:373-404) ----
         const Base b = particle_base(P, x[0], x[1], x[2], bad);
         const int lx = b.b[0] - bx * 4, ly = b.b[1] - by * 4, lz = b.b[2] - bz * 4;
@@ -755,26 +742,24 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_g2p2g(const M
               }
         }
         if (active) {
+          using R = PRows<Q>;
           if (mat != 4) {  // :406-408
 #pragma unroll
-            for (int d = 0; d < 3; ++d) {
-              v[d] = nv[d];
-              x[d] = x[d] + dt * v[d];
-            }
+            for (int d = 0; d < 3; ++d) v[d] = nv[d];
+            st_v<Q>(nxt, cap, j, v, bad);  // packed: the advection and P2G read the rounded v
+#pragma unroll
+            for (int d = 0; d < 3; ++d) x[d] = x[d] + dt * v[d];
+            st_x<Q>(nxt, cap, j, x, bad);
+          } else {
+            st_v<Q>(nxt, cap, j, v, bad);  // loaded values re-encode to the same words
+            st_x<Q>(nxt, cap, j, x, bad);
           }
           // ---- constitutive update and P2G at the new x (:410-485) ----
-          const P2GOut o = constitutive<true>(P, dt, mat, Ep, F, Jp, C);
-#pragma unroll
-          for (int d = 0; d < 3; ++d) {
-            dst[(kX + d) * cap] = x[d];
-            dst[(kV + d) * cap] = v[d];
-          }
-#pragma unroll
-          for (int a = 0; a < 9; ++a) dst[(kF + a) * cap] = F[a / 3][a % 3];
-          dst[kJp * cap] = Jp;
-          dst[kMat * cap] = __int_as_float(matword);
-          dst[kId * cap] = idf;
-          if (P.has_Ep) dst[kEp * cap] = Ep;
+          const P2GOut o = constitutive<true, Q>(P, dt, mat, Ep, F, Jp, C);
+          st_F_mat<Q>(nxt, cap, j, F, matword);
+          nxt[R::Jp * cap + j] = Jp;
+          nxt[R::Id * cap + j] = idf;
+          if (P.has_Ep) nxt[R::Ep * cap + j] = Ep;
           vmax = fmaxf(vmax, fmaxf(fabsf(v[0]), fmaxf(fabsf(v[1]), fabsf(v[2]))));
           const Base b2 = particle_base(P, x[0], x[1], x[2], bad);
           bspline_weights(b2.fx, wt);
@@ -904,6 +889,7 @@ struct DevInfo {
   int sms = 0;
   int p2g_ctas = 0, p2g_ep_ctas = 0, g2p_ctas = 0, g2p2g_ctas = 0;
   int p2g_b_ctas = 0, p2g_ep_b_ctas = 0, g2p_b_ctas = 0;
+  int p2g_q_ctas = 0, p2g_ep_q_ctas = 0, g2p_q_ctas = 0, g2p2g_q_ctas = 0;  // packed storage
 };
 
 static DevInfo g_dev[64];
@@ -918,15 +904,23 @@ static const DevInfo *dev_info() {
     int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return nullptr;
     int a = 0, b = 0, c = 0, a2 = 0, b2 = 0, c2 = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_p2g<false, false>, kP2GThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_p2g<true, false>, kP2GThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_g2p<false>, kG2PThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a2, k_p2g<false, true>, kP2GThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_p2g<true, true>, kP2GThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c2, k_g2p<true>, kG2PThreads, 0);
-    int f = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, k_g2p2g, kP2GThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_p2g<false, false, false>, kP2GThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_p2g<true, false, false>, kP2GThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_g2p<false, false>, kG2PThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a2, k_p2g<false, true, false>, kP2GThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_p2g<true, true, false>, kP2GThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c2, k_g2p<true, false>, kG2PThreads, 0);
+    int f = 0, aq = 0, bq = 0, cq = 0, fq = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, k_g2p2g<false>, kP2GThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&aq, k_p2g<false, false, true>, kP2GThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bq, k_p2g<true, false, true>, kP2GThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cq, k_g2p<false, true>, kG2PThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fq, k_g2p2g<true>, kP2GThreads, 0);
     d.g2p2g_ctas = sms * (f > 0 ? f : 1);
+    d.p2g_q_ctas = sms * (aq > 0 ? aq : 1);
+    d.p2g_ep_q_ctas = sms * (bq > 0 ? bq : 1);
+    d.g2p_q_ctas = sms * (cq > 0 ? cq : 1);
+    d.g2p2g_q_ctas = sms * (fq > 0 ? fq : 1);
     d.p2g_ctas = sms * (a > 0 ? a : 1);
     d.p2g_ep_ctas = sms * (b > 0 ? b : 1);
     d.g2p_ctas = sms * (c > 0 ? c : 1);
@@ -1010,8 +1004,11 @@ int mpm_bin_count(const MpmParams *p, void *ws, int64_t cap, const float *pstate
   Ws w;
   ws_layout(*p, cap, (char *)ws, &w);
   const int64_t n = end - begin;
-  k_bin_count<false><<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(*p, nullptr, w, pstate, cap, begin,
-                                                                                   end);
+  const unsigned nb = (unsigned)((n + 255) / 256);
+  if (p->quant)
+    k_bin_count<false, true><<<nb, 256, 0, (cudaStream_t)stream>>>(*p, nullptr, w, pstate, cap, begin, end);
+  else
+    k_bin_count<false, false><<<nb, 256, 0, (cudaStream_t)stream>>>(*p, nullptr, w, pstate, cap, begin, end);
   return last_error();
 }
 
@@ -1039,10 +1036,16 @@ int mpm_p2g(const MpmParams *p, void *ws, int64_t cap, int64_t n, const float *c
   Ws w;
   ws_layout(*p, cap, (char *)ws, &w);
   cudaStream_t s = (cudaStream_t)stream;
-  if (p->has_Ep)
-    k_p2g<true, false><<<di->p2g_ep_ctas, kP2GThreads, 0, s>>>(*p, nullptr, w, cur, nxt, cap, dt);
-  else
-    k_p2g<false, false><<<di->p2g_ctas, kP2GThreads, 0, s>>>(*p, nullptr, w, cur, nxt, cap, dt);
+  if (p->quant) {
+    if (p->has_Ep)
+      k_p2g<true, false, true><<<di->p2g_ep_q_ctas, kP2GThreads, 0, s>>>(*p, nullptr, w, cur, nxt, cap, dt);
+    else
+      k_p2g<false, false, true><<<di->p2g_q_ctas, kP2GThreads, 0, s>>>(*p, nullptr, w, cur, nxt, cap, dt);
+  } else if (p->has_Ep) {
+    k_p2g<true, false, false><<<di->p2g_ep_ctas, kP2GThreads, 0, s>>>(*p, nullptr, w, cur, nxt, cap, dt);
+  } else {
+    k_p2g<false, false, false><<<di->p2g_ctas, kP2GThreads, 0, s>>>(*p, nullptr, w, cur, nxt, cap, dt);
+  }
   return last_error();
 }
 
@@ -1063,13 +1066,18 @@ int mpm_g2p(const MpmParams *p, void *ws, int64_t cap, int64_t n, float *nxt, fl
   if (!di) return MPM_E_CUDA;
   Ws w;
   ws_layout(*p, cap, (char *)ws, &w);
-  k_g2p<false><<<di->g2p_ctas, kG2PThreads, 0, (cudaStream_t)stream>>>(*p, nullptr, w, nxt, cap, dt, maxv_out);
+  if (p->quant)
+    k_g2p<false, true><<<di->g2p_q_ctas, kG2PThreads, 0, (cudaStream_t)stream>>>(*p, nullptr, w, nxt, cap, dt,
+                                                                                 maxv_out);
+  else
+    k_g2p<false, false><<<di->g2p_ctas, kG2PThreads, 0, (cudaStream_t)stream>>>(*p, nullptr, w, nxt, cap, dt,
+                                                                                maxv_out);
   return last_error();
 }
 
 int mpm_g2p_bin_into(const MpmParams *p, void *ws, void *ws_bins, int64_t cap, int64_t n, float *nxt, float dt,
                      float *maxv_out, void *stream) {
-  if (!params_ok(p) || !ws || !ws_bins || !nxt || n < 0 || n > cap) return MPM_E_INVALID;
+  if (!params_ok(p) || p->quant || !ws || !ws_bins || !nxt || n < 0 || n > cap) return MPM_E_INVALID;
   const DevInfo *di = dev_info();
   if (!di) return MPM_E_CUDA;
   Ws w, wb;
@@ -1080,7 +1088,7 @@ int mpm_g2p_bin_into(const MpmParams *p, void *ws, void *ws_bins, int64_t cap, i
   w.cell_cnt = wb.cell_cnt;
   w.blk_flag = wb.blk_flag;
   w.cellkey = wb.cellkey;
-  k_g2p<false><<<di->g2p_ctas, kG2PThreads, 0, (cudaStream_t)stream>>>(*p, nullptr, w, nxt, cap, dt, maxv_out);
+  k_g2p<false, false><<<di->g2p_ctas, kG2PThreads, 0, (cudaStream_t)stream>>>(*p, nullptr, w, nxt, cap, dt, maxv_out);
   return last_error();
 }
 
@@ -1097,7 +1105,12 @@ int mpm_g2p2g_substep(const MpmParams *p, void *ws, int64_t cap, int64_t n, cons
   }
   Ws w;
   ws_layout(*p, cap, (char *)ws, &w);
-  k_g2p2g<<<di->g2p2g_ctas, kP2GThreads, 0, (cudaStream_t)stream>>>(*p, w, cur, nxt, cap, dt, first_new, maxv_out);
+  if (p->quant)
+    k_g2p2g<true><<<di->g2p2g_q_ctas, kP2GThreads, 0, (cudaStream_t)stream>>>(*p, w, cur, nxt, cap, dt, first_new,
+                                                                              maxv_out);
+  else
+    k_g2p2g<false><<<di->g2p2g_ctas, kP2GThreads, 0, (cudaStream_t)stream>>>(*p, w, cur, nxt, cap, dt, first_new,
+                                                                             maxv_out);
   rc = last_error();
   if (rc) return rc;
   rc = mpm_bin_finalize(p, ws, cap, n, stream);
@@ -1117,7 +1130,7 @@ int mpm_substep(const MpmParams *p, void *ws, int64_t cap, int64_t n, const floa
 }
 
 static bool batch_ok(const MpmParams *p) {
-  if (!params_ok(p) || p->n_scenes < 1) return false;
+  if (!params_ok(p) || p->n_scenes < 1 || p->quant) return false;
   int64_t slots = 1;
   for (int d = 0; d < 3; ++d) {
     if (p->slot_nb[d] <= 0 || p->slots[d] <= 0) return false;
@@ -1134,8 +1147,8 @@ int mpm_batch_bin_count(const MpmParams *p, const MpmParams *scenes, void *ws, i
   Ws w;
   ws_layout(*p, cap, (char *)ws, &w);
   const int64_t n = end - begin;
-  k_bin_count<true><<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(*p, scenes, w, pstate, cap, begin,
-                                                                                  end);
+  k_bin_count<true, false><<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(*p, scenes, w, pstate, cap,
+                                                                                         begin, end);
   return last_error();
 }
 
@@ -1150,17 +1163,17 @@ int mpm_batch_substep(const MpmParams *p, const MpmParams *scenes, void *ws, int
   ws_layout(*p, cap, (char *)ws, &w);
   cudaStream_t s = (cudaStream_t)stream;
   if (p->has_Ep)
-    k_p2g<true, true><<<di->p2g_ep_b_ctas, kP2GThreads, 0, s>>>(*p, scenes, w, cur, nxt, cap, 0.0f);
+    k_p2g<true, true, false><<<di->p2g_ep_b_ctas, kP2GThreads, 0, s>>>(*p, scenes, w, cur, nxt, cap, 0.0f);
   else
-    k_p2g<false, true><<<di->p2g_b_ctas, kP2GThreads, 0, s>>>(*p, scenes, w, cur, nxt, cap, 0.0f);
+    k_p2g<false, true, false><<<di->p2g_b_ctas, kP2GThreads, 0, s>>>(*p, scenes, w, cur, nxt, cap, 0.0f);
   k_grid<true><<<di->sms * 8, 256, 0, s>>>(*p, scenes, w, 0.0f);
-  k_g2p<true><<<di->g2p_b_ctas, kG2PThreads, 0, s>>>(*p, scenes, w, nxt, cap, 0.0f, maxv_out);
+  k_g2p<true, false><<<di->g2p_b_ctas, kG2PThreads, 0, s>>>(*p, scenes, w, nxt, cap, 0.0f, maxv_out);
   return last_error();
 }
 
 int mpm_substep_noalloc(const MpmParams *p, int64_t cap, int64_t n, const float *cur, float *nxt, float dt,
                         float *maxv_out, void *stream) {
-  if (!params_ok(p) || !cur || !nxt || n < 0 || n > cap) return MPM_E_INVALID;
+  if (!params_ok(p) || p->quant || !cur || !nxt || n < 0 || n > cap) return MPM_E_INVALID;
   if (n > kStaticMaxParticles) return MPM_E_CAPACITY;
   const size_t bytes = ws_layout(*p, kStaticMaxParticles, nullptr, nullptr);
   if (bytes > kStaticScratchBytes) return MPM_E_CAPACITY;
@@ -1176,7 +1189,7 @@ int mpm_substep_noalloc(const MpmParams *p, int64_t cap, int64_t n, const float 
   // block flags, cell counters and grids this call relies on.
   if (cudaMemsetAsync(base, 0, bytes, s) != cudaSuccess) return MPM_E_CUDA;
   if (n > 0) {
-    k_bin_count<false><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(*p, nullptr, w, cur, cap, 0, n);
+    k_bin_count<false, false><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(*p, nullptr, w, cur, cap, 0, n);
     k_flags_count<<<w.nflagtiles, 256, 0, s>>>(*p, w);
     k_flags_write<<<w.nflagtiles, 256, 0, s>>>(*p, w);
     k_pb_stats<<<w.nstattiles, 256, 0, s>>>(*p, w);
@@ -1184,11 +1197,11 @@ int mpm_substep_noalloc(const MpmParams *p, int64_t cap, int64_t n, const float 
     k_pb_levels<<<di->sms * 8, 256, 0, s>>>(*p, w, kStaticMaxParticles);
     k_scatter<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(*p, w, n);
     if (p->has_Ep)
-      k_p2g<true, false><<<di->p2g_ep_ctas, kP2GThreads, 0, s>>>(*p, nullptr, w, cur, nxt, cap, dt);
+      k_p2g<true, false, false><<<di->p2g_ep_ctas, kP2GThreads, 0, s>>>(*p, nullptr, w, cur, nxt, cap, dt);
     else
-      k_p2g<false, false><<<di->p2g_ctas, kP2GThreads, 0, s>>>(*p, nullptr, w, cur, nxt, cap, dt);
+      k_p2g<false, false, false><<<di->p2g_ctas, kP2GThreads, 0, s>>>(*p, nullptr, w, cur, nxt, cap, dt);
     k_grid<false><<<di->sms * 8, 256, 0, s>>>(*p, nullptr, w, dt);
-    k_g2p<false><<<di->g2p_ctas, kG2PThreads, 0, s>>>(*p, nullptr, w, nxt, cap, dt, maxv_out);
+    k_g2p<false, false><<<di->g2p_ctas, kG2PThreads, 0, s>>>(*p, nullptr, w, nxt, cap, dt, maxv_out);
   }
   return last_error();
 }

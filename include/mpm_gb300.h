@@ -272,17 +272,18 @@ int mpm_substep_noalloc(const MpmParams *p, int64_t cap, int64_t n, const float 
 int mpm_gather_rows(const float *pstate, int64_t cap, int64_t n, int32_t row0, int32_t ncols,
                     float *out, void *stream);
 
-/* Packed particle storage (quant=True).  mpm_quant_pack encodes slots
- * [begin, end) of a float32-layout buffer (MPM_NROWS rows of stride
- * rows_cap) into the packed buffer (MPM_QROWS rows of stride cap), rounding
- * to the nearest representable value (ties away from zero); positions
- * outside [-2, 2) are clamped and OR MPM_STATUS_OUT_OF_GRID into *status
- * (device int32, may be null), non-finite values MPM_STATUS_NONFINITE.
- * mpm_quant_unpack decodes the same slots back into the float32 layout
- * (rows 25 and 26 carry the material and id as int32 bits). */
-int mpm_quant_pack(const float *rows, int64_t rows_cap, int64_t begin, int64_t end, float *packed, int64_t cap,
+/* Packed particle storage (quant=True).  mpm_quant_pack encodes `count`
+ * slots of a float32-layout buffer (MPM_NROWS rows of stride rows_cap, slot
+ * t at column t) into slots begin + t of the packed buffer (MPM_QROWS rows of
+ * stride cap), rounding to the nearest representable value (ties away from
+ * zero); positions outside [-2, 2) are clamped and OR MPM_STATUS_OUT_OF_GRID
+ * into *status (device int32, may be null), non-finite values
+ * MPM_STATUS_NONFINITE.  mpm_quant_unpack decodes packed slots begin + t
+ * into column t of a float32-layout buffer (rows 25 and 26 carry the
+ * material and id as int32 bits). */
+int mpm_quant_pack(const float *rows, int64_t rows_cap, int64_t count, float *packed, int64_t cap, int64_t begin,
                    int32_t *status, void *stream);
-int mpm_quant_unpack(const float *packed, int64_t cap, int64_t begin, int64_t end, float *rows, int64_t rows_cap,
+int mpm_quant_unpack(const float *packed, int64_t cap, int64_t begin, int64_t count, float *rows, int64_t rows_cap,
                      void *stream);
 
 /* ---- Particle output (engine/particle_io.py:12-76, ParticleIO.write_particles)

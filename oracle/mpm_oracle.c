@@ -8,11 +8,12 @@
  *
  * Exported symbols carry a _d (float64) or _f (float32) suffix.
  *
- * `pd` (double[16]) layout, ORACLE_PD_*:
+ * `pd` (double[17]) layout, ORACLE_PD_*:
  *   0 dx, 1 inv_dx, 2 p_vol, 3 p_mass, 4 mu0, 5 la0, 6 alpha (sand),
  *   7 water_density, 8..10 gravity, 11 p_vol*4*inv_dx^2, 12 (3la0+2mu0)/(2mu0),
  *   13 nu, 14 support_plasticity (0 or 1), 15 dx * g2p2g_allowed_cfl of the
- *   fused mode's grid velocity clamp (0 = none)
+ *   fused mode's grid velocity clamp (0 = none), 16 quant (0 or 1: stored
+ *   x, v and F take the values of the packed fields)
  * Post-process records (double[12] each), applied in list order like the
  *   reference's grid_postprocess list: 0 kind (0 plane, 1 sphere,
  *   2 bounding box), 1 surface (0 sticky, 1 slip, 2 separate; for the box:

@@ -39,6 +39,8 @@
 #define LOG(x) logf(x)
 #define FABS(x) fabsf(x)
 #define FLOOR(x) floorf(x)
+#define FREXP(x, e) frexpf(x, e)
+#define LDEXP(x, e) ldexpf(x, e)
 #define SVD_SWEEPS 5
 #else
 #define RSQRT(x) (1.0 / sqrt(x))
@@ -47,6 +49,8 @@
 #define LOG(x) log(x)
 #define FABS(x) fabs(x)
 #define FLOOR(x) floor(x)
+#define FREXP(x, e) frexp(x, e)
+#define LDEXP(x, e) ldexp(x, e)
 #define SVD_SWEEPS 40
 #endif
 
@@ -58,6 +62,7 @@ typedef struct {
   REAL nu;
   int plasticity; /* support_plasticity (engine/mpm_solver.py:62) */
   REAL v_clamp_k; /* dx * g2p2g_allowed_cfl, or 0 (no grid velocity clamp) */
+  int quant;      /* quant=True: stored x, v, F rounded to the packed formats */
 } FN(Consts);
 
 static void FN(make_consts)(const double *pd, FN(Consts) * c) {
@@ -78,6 +83,70 @@ static void FN(make_consts)(const double *pd, FN(Consts) * c) {
   c->nu = (REAL)pd[13];
   c->plasticity = pd[14] != 0.0;
   c->v_clamp_k = (REAL)pd[15];
+  c->quant = pd[16] != 0.0;
+}
+
+/* ------------------------------------------- quantized storage values --- */
+
+/* The values the packed fields of quant=True hold (engine/mpm_solver.py
+ * :106-116): x as signed 21-bit fixed point of scale 2^-19 (range [-2, 2)),
+ * F as signed 16-bit fixed point of scale 4.1 / 2^15 (F_bound + 0.1), v as
+ * block floating point: one exponent for the vector, unit 2^u with
+ * u = clamp(k - 18, -100, 27) where max |v_d| lies in [2^(k-1), 2^k), and
+ * signed 19-bit mantissas (|m| <= 2^18 - 1; a rounding carry to 2^18 moves
+ * to the next unit).  Rounding to nearest, ties away from zero; out-of-range
+ * values saturate; non-finite values become 0. */
+static REAL FN(q_round)(REAL s) {
+  REAL t = s + (s < (REAL)0 ? (REAL)-0.5 : (REAL)0.5);
+  if (t >= (REAL)2147483648.0) return (REAL)2147483647.0; /* saturates like the device's int32 conversion */
+  if (t <= (REAL)-2147483648.0) return (REAL)-2147483648.0;
+  return (REAL)(int64_t)t;
+}
+
+static REAL FN(q_x)(REAL x) {
+  if (!isfinite(x)) return 0;
+  REAL q = FN(q_round)(x * (REAL)524288.0);
+  if (q < (REAL)-1048576.0) q = (REAL)-1048576.0;
+  if (q > (REAL)1048575.0) q = (REAL)1048575.0;
+  return q * (REAL)(1.0 / 524288.0);
+}
+
+static REAL FN(q_F)(REAL f) {
+  if (!isfinite(f)) return 0;
+  REAL q = FN(q_round)(f * (REAL)(32768.0 / 4.1));
+  if (q < (REAL)-32768.0) q = (REAL)-32768.0;
+  if (q > (REAL)32767.0) q = (REAL)32767.0;
+  return q * (REAL)(4.1 / 32768.0);
+}
+
+static void FN(q_v)(REAL *v) {
+  if (!isfinite(v[0]) || !isfinite(v[1]) || !isfinite(v[2])) {
+    v[0] = v[1] = v[2] = 0;
+    return;
+  }
+  REAL M = FABS(v[0]);
+  if (FABS(v[1]) > M) M = FABS(v[1]);
+  if (FABS(v[2]) > M) M = FABS(v[2]);
+  int k = -126;
+  if (M > (REAL)0) (void)FREXP(M, &k);
+  int u = k - 18;
+  if (u < -100) u = -100;
+  if (u > 27) u = 27;
+  REAL m[3];
+  for (int pass = 0; pass < 2; ++pass) {
+    REAL big = 0;
+    for (int d = 0; d < 3; ++d) {
+      m[d] = FN(q_round)(LDEXP(v[d], -u));
+      if (FABS(m[d]) > big) big = FABS(m[d]);
+    }
+    if (big < (REAL)262144.0 || u == 27) break;
+    ++u;
+  }
+  for (int d = 0; d < 3; ++d) {
+    if (m[d] > (REAL)262143.0) m[d] = (REAL)262143.0;
+    if (m[d] < (REAL)-262143.0) m[d] = (REAL)-262143.0;
+    v[d] = LDEXP(m[d], u);
+  }
 }
 
 /* ---------------------------------------------------------------- SVD --- */
@@ -287,6 +356,13 @@ static void FN(p2g_particle)(const FN(Consts) * k, REAL dt, int mat, REAL Ep,
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) G[i][j] = (REAL)(i == j) + dt * C[i][j];
   FN(matmul3)(G, F, Fn); /* :513 */
+  if (fused && k->quant) { /* :413-417: clamp to F_bound, stored (rounded) F read back */
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        REAL f = Fn[i][j] < (REAL)-4 ? (REAL)-4 : (Fn[i][j] > (REAL)4 ? (REAL)4 : Fn[i][j]);
+        Fn[i][j] = FN(q_F)(f);
+      }
+  }
   REAL h = 1;
   if (k->plasticity && (fused || mat != 0)) h = EXP((REAL)10 * ((REAL)1 - *Jp)); /* :516-518, :427-429 */
   if (mat == 1) h = (REAL)0.3;                         /* :519-521 */
@@ -319,10 +395,12 @@ static void FN(p2g_particle)(const FN(Consts) * k, REAL dt, int mat, REAL Ep,
       for (int j = 0; j < 3; ++j) Fn[i][j] = (REAL)(i == j);
     Fn[0][0] = J;
     if (!fused && k->plasticity) *Jp = J;
-  } else if (mat == 2) { /* :543-545 */
+  } else if (mat == 2) { /* :543-545 (fused :446-447) */
     for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j)
+      for (int j = 0; j < 3; ++j) {
         Fn[i][j] = U[i][0] * sg[0] * V[j][0] + U[i][1] * sg[1] * V[j][1] + U[i][2] * sg[2] * V[j][2];
+        if (fused && k->quant) Fn[i][j] = FN(q_F)(Fn[i][j]);
+      }
   }
   if (mat != 3) { /* :549-551 */
     REAL R[3][3], D[3][3];
@@ -341,8 +419,10 @@ static void FN(p2g_particle)(const FN(Consts) * k, REAL dt, int mat, REAL Ep,
   } else { /* :552-566 */
     FN(sand_projection)(sg, Jp, k, mu0, la0);
     for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j)
+      for (int j = 0; j < 3; ++j) {
         Fn[i][j] = U[i][0] * sg[0] * V[j][0] + U[i][1] * sg[1] * V[j][1] + U[i][2] * sg[2] * V[j][2];
+        if (fused && k->quant) Fn[i][j] = FN(q_F)(Fn[i][j]); /* :458 */
+      }
     REAL ls = 0, cen[3];
     for (int i = 0; i < 3; ++i) {
       REAL l = LOG(sg[i]);
@@ -358,7 +438,7 @@ static void FN(p2g_particle)(const FN(Consts) * k, REAL dt, int mat, REAL Ep,
       for (int j = 0; j < 3; ++j) stress[i][j] = T[i][0] * Fn[j][0] + T[i][1] * Fn[j][1] + T[i][2] * Fn[j][2];
   }
   for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) F9[3 * i + j] = Fn[i][j]; /* :567 */
+    for (int j = 0; j < 3; ++j) F9[3 * i + j] = k->quant ? FN(q_F)(Fn[i][j]) : Fn[i][j]; /* :567 */
   REAL sc = -dt * k->stress_scale_k;                     /* :569 */
   REAL mass = k->p_mass;
   if (!fused && mat == 0) mass *= k->water_density; /* :571-573 */
@@ -488,7 +568,7 @@ static void FN(grid_node)(int gi, int gj, int gk, REAL m, REAL *v, REAL dt, cons
 
 /* G2P for one particle: engine/mpm_solver.py:701-724 */
 static int FN(g2p_particle)(const FN(Window) * w, const FN(Consts) * k, REAL dt, int mat,
-                            REAL *xp, REAL *vp, REAL *C9, const REAL *gv) {
+                            REAL *xp, REAL *vp, REAL *C9, const REAL *gv, int quant) {
   int32_t base[3];
   REAL fx[3], wt[3][3];
   FN(base_cell)(xp, k->inv_dx, base, fx);
@@ -511,14 +591,27 @@ static int FN(g2p_particle)(const FN(Window) * w, const FN(Consts) * k, REAL dt,
       }
   if (mat != 4) {
     for (int d = 0; d < 3; ++d) vp[d] = nv[d];
+    if (quant) FN(q_v)(vp); /* the advection reads the stored v */
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) C9[3 * i + j] = nC[i][j];
     for (int d = 0; d < 3; ++d) xp[d] += dt * vp[d];
+    if (quant)
+      for (int d = 0; d < 3; ++d) xp[d] = FN(q_x)(xp[d]);
   }
   return 0;
 }
 
 /* ------------------------------------------------------- public API ----- */
+
+/* The stored values of quant=True for n particles, in place: x (n*3),
+ * v (n*3, one shared exponent per particle) and F (n*9). */
+void FN(oracle_quant_values)(int64_t n, REAL *x, REAL *v, REAL *F) {
+  for (int64_t p = 0; p < n; ++p) {
+    for (int d = 0; d < 3; ++d) x[3 * p + d] = FN(q_x)(x[3 * p + d]);
+    FN(q_v)(v + 3 * p);
+    for (int a = 0; a < 9; ++a) F[9 * p + a] = FN(q_F)(F[9 * p + a]);
+  }
+}
 
 /* P2G over all particles into a zeroed dense window grid. Returns the number
  * of particles whose stencil left the window (0 on success). */
@@ -574,7 +667,7 @@ int FN(oracle_g2p)(const double *pd, int64_t n, REAL *x, REAL *v, REAL *C, const
   int bad = 0;
 #pragma omp parallel for num_threads(nthreads) schedule(static) reduction(+ : bad)
   for (int64_t p = 0; p < n; ++p)
-    bad += FN(g2p_particle)(&w, &k, dt, mat[p], x + 3 * p, v + 3 * p, C + 9 * p, gv);
+    bad += FN(g2p_particle)(&w, &k, dt, mat[p], x + 3 * p, v + 3 * p, C + 9 * p, gv, k.quant);
   return bad;
 }
 
@@ -606,15 +699,17 @@ int FN(oracle_g2p2g)(const double *pd, const int32_t *res, int padding, int unbo
       /* the gather of g2p_particle, applied to scratch copies (mat 0 so that
        * it writes v and C; x is advected below) */
       REAL xg[3] = {xs[0], xs[1], xs[2]};
-      if (FN(g2p_particle)(&w, &k, (REAL)0, 0, xg, nv, C9, gv_in)) {
+      if (FN(g2p_particle)(&w, &k, (REAL)0, 0, xg, nv, C9, gv_in, 0)) {
         bad += 1;
         continue;
       }
     }
     if (mat[p] != 4) {
+      if (k.quant) FN(q_v)(nv); /* :405-408 read the stored v */
       for (int d = 0; d < 3; ++d) {
         v[3 * p + d] = nv[d];
         x[3 * p + d] += dt * v[3 * p + d];
+        if (k.quant) x[3 * p + d] = FN(q_x)(x[3 * p + d]);
       }
     }
     REAL affine[3][3], mass;
@@ -719,7 +814,7 @@ int FN(oracle_substeps)(const double *pd, const int32_t *res, int padding, int u
     REAL mv = 0;
 #pragma omp parallel for num_threads(nthreads) schedule(static) reduction(max : mv)
     for (int64_t p = 0; p < n; ++p) {
-      FN(g2p_particle)(&w, &k, dt, mat[p], x + 3 * p, v + 3 * p, C + 9 * p, gmv);
+      FN(g2p_particle)(&w, &k, dt, mat[p], x + 3 * p, v + 3 * p, C + 9 * p, gmv, k.quant);
       for (int d = 0; d < 3; ++d) {
         REAL a = FABS(v[3 * p + d]);
         if (a > mv) mv = a;
@@ -750,5 +845,7 @@ int FN(oracle_substeps)(const double *pd, const int32_t *res, int padding, int u
 #undef LOG
 #undef FABS
 #undef FLOOR
+#undef FREXP
+#undef LDEXP
 #undef SVD_SWEEPS
 #undef FN

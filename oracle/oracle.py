@@ -66,6 +66,8 @@ def lib() -> ctypes.CDLL:
             getattr(L, "oracle_g2p2g" + sfx).argtypes = [vp, vp, i32, i32, i32, i32, vp, i64, i64, vp, vp, vp, vp,
                                                          vp, vp, real, vp, vp, vp, vp, vp]
             getattr(L, "oracle_g2p2g" + sfx).restype = i32
+            getattr(L, "oracle_quant_values" + sfx).argtypes = [i64, vp, vp, vp]
+            getattr(L, "oracle_quant_values" + sfx).restype = None
         _lib = L
     return _lib
 
@@ -88,6 +90,8 @@ class Config:
     support_plasticity: bool = True
     # fused G2P2G mode: grid velocities clamped to +-cfl * dx / dt (0 = off)
     v_clamp_cfl: float = 0.0
+    # quant=True: stored x, v, F rounded to the packed formats
+    quant: bool = False
     # grid_postprocess list; the bounding box first, as the constructor adds it
     postprocess: list = field(default_factory=lambda: [dict(kind=KIND_BOX, surface=0)])
 
@@ -115,7 +119,7 @@ class Config:
             self.dx, self.inv_dx, self.p_vol, self.p_mass, self.mu_0, self.lambda_0, self.alpha, self.water_density,
             self.gravity[0], self.gravity[1], self.gravity[2], self.p_vol * 4 * self.inv_dx**2,
             (3 * self.lambda_0 + 2 * self.mu_0) / (2 * self.mu_0), self.nu, float(bool(self.support_plasticity)),
-            self.dx * self.v_clamp_cfl
+            self.dx * self.v_clamp_cfl, float(bool(self.quant))
         ], dtype=np.float64)
 
     def coll(self) -> np.ndarray:
@@ -296,6 +300,16 @@ def substep(cfg: Config, P: Particles, dt: float, win: Window | None = None, nth
     gv = grid_update(cfg, gm, gmv, dt, win, nthreads)
     g2p(cfg, P, gv, dt, win, nthreads)
     return win, gm, gmv, gv
+
+
+def quant_values(x, v, F):
+    """The values quant=True stores for positions (n,3), velocities (n,3)
+    and deformation gradients (n,3,3): copies of the same dtype
+    (float64 or float32)."""
+    x, v, F = (np.ascontiguousarray(a).copy() for a in (x, v, F))
+    sfx = "_d" if x.dtype == np.float64 else "_f"
+    getattr(lib(), "oracle_quant_values" + sfx)(x.shape[0], _p(x), _p(v), _p(F))
+    return x, v, F
 
 
 class Runner:

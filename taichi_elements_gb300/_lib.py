@@ -132,7 +132,7 @@ SIGNATURES = {
     "mpm_p2g_adj": [_P, _v, _i64, _i64, _v, _f, _v, _v, _v, _v, _i32, _v],
     "mpm_batch_substep": [_P, _v, _v, _i64, _i64, _v, _v, _v, _v],
     "mpm_gather_rows": [_v, _i64, _i64, _i32, _i32, _v, _v],
-    "mpm_quant_pack": [_v, _i64, _i64, _i64, _v, _i64, _v, _v],
+    "mpm_quant_pack": [_v, _i64, _i64, _v, _i64, _i64, _v, _v],
     "mpm_quant_unpack": [_v, _i64, _i64, _i64, _v, _i64, _v],
     "mpm_status_ptr": [_P, _v, _i64, ctypes.POINTER(ctypes.c_void_p)],
     "mpm_max_grid_velocity": [_P, _v, _i64, _v, _v],

@@ -129,38 +129,40 @@ __global__ __launch_bounds__(kIoThreads) void k_unpack_colors(const int32_t *__r
 // quant=True (quant.cuh).  Both keep the slot order.
 
 __global__ __launch_bounds__(kIoThreads) void k_quant_pack(const float *__restrict__ rows, int64_t rows_cap,
-                                                           int64_t begin, int64_t end, float *__restrict__ pk,
-                                                           int64_t cap, int32_t *status) {
-  const int64_t j = begin + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+                                                           int64_t count, float *__restrict__ pk, int64_t cap,
+                                                           int64_t begin, int32_t *status) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t j = begin + t;
   uint32_t bad = 0;
-  if (j < end) {
+  if (t < count) {
     using R = PRows<true>;
     using L = PRows<false>;
     float x[3], v[3], F[3][3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-      x[d] = rows[(L::X + d) * rows_cap + j];
-      v[d] = rows[(L::V + d) * rows_cap + j];
+      x[d] = rows[(L::X + d) * rows_cap + t];
+      v[d] = rows[(L::V + d) * rows_cap + t];
     }
 #pragma unroll
-    for (int a = 0; a < 9; ++a) F[a / 3][a % 3] = rows[(L::F + a) * rows_cap + j];
+    for (int a = 0; a < 9; ++a) F[a / 3][a % 3] = rows[(L::F + a) * rows_cap + t];
     st_x<true>(pk, cap, j, x, bad);
     st_v<true>(pk, cap, j, v, bad);
-    st_F_mat<true>(pk, cap, j, F, __float_as_int(rows[L::Mat * rows_cap + j]));
-    pk[R::Jp * cap + j] = rows[L::Jp * rows_cap + j];
-    pk[R::Id * cap + j] = rows[L::Id * rows_cap + j];
-    pk[R::Ep * cap + j] = rows[L::Ep * rows_cap + j];
+    st_F_mat<true>(pk, cap, j, F, __float_as_int(rows[L::Mat * rows_cap + t]));
+    pk[R::Jp * cap + j] = rows[L::Jp * rows_cap + t];
+    pk[R::Id * cap + j] = rows[L::Id * rows_cap + t];
+    pk[R::Ep * cap + j] = rows[L::Ep * rows_cap + t];
 #pragma unroll
-    for (int a = 0; a < 9; ++a) pk[(R::C + a) * cap + j] = rows[(L::C + a) * rows_cap + j];
+    for (int a = 0; a < 9; ++a) pk[(R::C + a) * cap + j] = rows[(L::C + a) * rows_cap + t];
   }
   if (status && bad) atomicOr(status, (int32_t)bad);
 }
 
 __global__ __launch_bounds__(kIoThreads) void k_quant_unpack(const float *__restrict__ pk, int64_t cap,
-                                                             int64_t begin, int64_t end, float *__restrict__ rows,
+                                                             int64_t begin, int64_t count, float *__restrict__ rows,
                                                              int64_t rows_cap) {
-  const int64_t j = begin + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= end) return;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const int64_t j = begin + t;
   using R = PRows<true>;
   using L = PRows<false>;
   float x[3], v[3], F[3][3];
@@ -169,18 +171,18 @@ __global__ __launch_bounds__(kIoThreads) void k_quant_unpack(const float *__rest
   ld_F<true>(pk, cap, j, F);
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    rows[(L::X + d) * rows_cap + j] = x[d];
-    rows[(L::V + d) * rows_cap + j] = v[d];
+    rows[(L::X + d) * rows_cap + t] = x[d];
+    rows[(L::V + d) * rows_cap + t] = v[d];
   }
 #pragma unroll
   for (int a = 0; a < 9; ++a) {
-    rows[(L::F + a) * rows_cap + j] = F[a / 3][a % 3];
-    rows[(L::C + a) * rows_cap + j] = pk[(R::C + a) * cap + j];
+    rows[(L::F + a) * rows_cap + t] = F[a / 3][a % 3];
+    rows[(L::C + a) * rows_cap + t] = pk[(R::C + a) * cap + j];
   }
-  rows[L::Mat * rows_cap + j] = __int_as_float(ld_mat<true>(pk, cap, j));
-  rows[L::Jp * rows_cap + j] = pk[R::Jp * cap + j];
-  rows[L::Id * rows_cap + j] = pk[R::Id * cap + j];
-  rows[L::Ep * rows_cap + j] = pk[R::Ep * cap + j];
+  rows[L::Mat * rows_cap + t] = __int_as_float(ld_mat<true>(pk, cap, j));
+  rows[L::Jp * rows_cap + t] = pk[R::Jp * cap + j];
+  rows[L::Id * rows_cap + t] = pk[R::Id * cap + j];
+  rows[L::Ep * rows_cap + t] = pk[R::Ep * cap + j];
 }
 
 }  // namespace mpm
@@ -227,21 +229,21 @@ int mpm_unpack_colors(const int32_t *color, int64_t n, uint8_t *rgb, void *strea
   return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_E_CUDA;
 }
 
-int mpm_quant_pack(const float *rows, int64_t rows_cap, int64_t begin, int64_t end, float *packed, int64_t cap,
+int mpm_quant_pack(const float *rows, int64_t rows_cap, int64_t count, float *packed, int64_t cap, int64_t begin,
                    int32_t *status, void *stream) {
-  if (!rows || !packed || begin < 0 || begin > end || end > cap || end > rows_cap) return MPM_E_INVALID;
-  if (end == begin) return MPM_OK;
-  k_quant_pack<<<(unsigned)((end - begin + kIoThreads - 1) / kIoThreads), kIoThreads, 0, (cudaStream_t)stream>>>(
-      rows, rows_cap, begin, end, packed, cap, status);
+  if (!rows || !packed || count < 0 || begin < 0 || count > rows_cap || begin + count > cap) return MPM_E_INVALID;
+  if (count == 0) return MPM_OK;
+  k_quant_pack<<<(unsigned)((count + kIoThreads - 1) / kIoThreads), kIoThreads, 0, (cudaStream_t)stream>>>(
+      rows, rows_cap, count, packed, cap, begin, status);
   return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_E_CUDA;
 }
 
-int mpm_quant_unpack(const float *packed, int64_t cap, int64_t begin, int64_t end, float *rows, int64_t rows_cap,
+int mpm_quant_unpack(const float *packed, int64_t cap, int64_t begin, int64_t count, float *rows, int64_t rows_cap,
                      void *stream) {
-  if (!rows || !packed || begin < 0 || begin > end || end > cap || end > rows_cap) return MPM_E_INVALID;
-  if (end == begin) return MPM_OK;
-  k_quant_unpack<<<(unsigned)((end - begin + kIoThreads - 1) / kIoThreads), kIoThreads, 0, (cudaStream_t)stream>>>(
-      packed, cap, begin, end, rows, rows_cap);
+  if (!rows || !packed || count < 0 || begin < 0 || count > rows_cap || begin + count > cap) return MPM_E_INVALID;
+  if (count == 0) return MPM_OK;
+  k_quant_unpack<<<(unsigned)((count + kIoThreads - 1) / kIoThreads), kIoThreads, 0, (cudaStream_t)stream>>>(
+      packed, cap, begin, count, rows, rows_cap);
   return cudaGetLastError() == cudaSuccess ? MPM_OK : MPM_E_CUDA;
 }
 

@@ -16,7 +16,8 @@
 //   row 9 Jp, row 10 id, row 11 E_p (float32 as above), rows 12-20 C.
 // Values are rounded to the nearest representable value, ties away from
 // zero.  Positions outside [-2, 2) raise the out-of-grid status and F
-// entries outside the range saturate.
+// entries outside the range saturate; non-finite values store 0 (and raise
+// the non-finite status for x and v).
 #pragma once
 
 #include <stdint.h>
@@ -45,9 +46,13 @@ __device__ __forceinline__ int32_t q_round(float s) {  // ties away from zero
   return __float2int_rz(__fadd_rn(s, copysignf(0.5f, s)));
 }
 
+// 16-bit code of one F entry: saturating, 0 for a non-finite value
+__device__ __forceinline__ int32_t qf_code(float v) {
+  return isfinite(v) ? max(-32768, min(32767, q_round(__fmul_rn(v, kQfInv)))) : 0;
+}
+
 __device__ __forceinline__ float q_fixed_F(float v) {  // quantize and decode one F entry
-  const int32_t q = max(-32768, min(32767, q_round(__fmul_rn(v, kQfInv))));
-  return __fmul_rn((float)q, kQfScale);
+  return __fmul_rn((float)qf_code(v), kQfScale);
 }
 
 __device__ __forceinline__ float pow2f(int u) {  // 2^u for u in [-126, 127]
@@ -225,7 +230,7 @@ __device__ __forceinline__ void st_F_mat(float *__restrict__ s, int64_t cap, int
     uint32_t h[10];
 #pragma unroll
     for (int a = 0; a < 9; ++a)
-      h[a] = (uint32_t)(uint16_t)max(-32768, min(32767, q_round(__fmul_rn(F[a / 3][a % 3], kQfInv))));
+      h[a] = (uint32_t)(uint16_t)qf_code(F[a / 3][a % 3]);
     h[9] = (uint32_t)matword & 0xFFFFu;
     uint32_t *u = reinterpret_cast<uint32_t *>(s + PRows<Q>::F * cap);
 #pragma unroll

@@ -45,9 +45,9 @@ class Rollout:
                  use_cuda_graph: bool = True, keep_workspaces: bool | None = None):
         if not solver.per_particle_E:
             raise ValueError("the differentiable rollout needs MPMSolver(per_particle_E=True)")
-        if not solver.support_plasticity or solver.use_g2p2g:
+        if not solver.support_plasticity or solver.use_g2p2g or solver.quant:
             raise NotImplementedError("gradients follow the default substep (support_plasticity=True, "
-                                      "use_g2p2g=False)")
+                                      "use_g2p2g=False, quant=False)")
         self.s = solver
         self.n_substeps = int(n_substeps)
         self.dt = float(dt if dt is not None else solver.default_dt)

@@ -19,6 +19,14 @@ modulus (``per_particle_E=True`` and the ``E`` argument of the seeding
 calls), ``state_dict``/``load_state_dict`` (exact checkpoints of x, v, C, F,
 Jp), ``tensors()`` (zero-copy device views), CUDA-graph capture of whole
 frames and a measured choice of the work-item size (``autotune=True``).
+
+``quant=True`` keeps the particles in the packed layout of the reference's
+quantized fields (engine/mpm_solver.py:106-127, :216-262): positions as
+21-bit fixed point in [-2, 2), velocities as block floating point (a 7-bit
+shared exponent and 19-bit mantissas), F as 16-bit fixed point of range
++-4.1 and the material in 16 bits; 84 bytes per particle instead of 112.
+``support_plasticity=False`` drops the Jp updates (:62 and the
+``ti.static(self.support_plasticity)`` branches).
 """
 from __future__ import annotations
 
@@ -31,7 +39,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from ._lib import (KIND_BOX, KIND_SPHERE, KIND_SURFACE, NROWS, ROW_C, ROW_EP, ROW_F, ROW_ID, ROW_JP, ROW_MAT,
+from ._lib import (KIND_BOX, KIND_SPHERE, KIND_SURFACE, NROWS, QROWS, ROW_C, ROW_EP, ROW_F, ROW_ID, ROW_JP, ROW_MAT,
                    ROW_V, ROW_X)
 
 
@@ -98,8 +106,6 @@ class MPMSolver:
         assert self.dim in (2, 3), "MPM solver supports only 2D and 3D simulations."
         if self.dim != 3:
             raise NotImplementedError("the GB300 engine implements the 3-D solver only")
-        if quant:
-            raise NotImplementedError("quantised particle storage (quant=True) is not implemented")
 
         self.device = torch.device(device if device is not None else "cuda")
         if self.device.type != "cuda" or not torch.cuda.is_available():
@@ -216,6 +222,7 @@ class MPMSolver:
         p.has_Ep = int(self.per_particle_E)
         p.chunk = self.chunk
         p.plasticity = int(bool(self.support_plasticity))
+        p.quant = int(bool(self.quant))
         p.dx = self.dx
         p.inv_dx = self.inv_dx
         p.p_vol = self.p_vol
@@ -310,7 +317,8 @@ class MPMSolver:
         """(Re)allocate particle buffers with capacity `cap`, keeping data."""
         cap = int((cap + 255) // 256 * 256)
         n = self.n_particles
-        new_state = [torch.zeros((NROWS, cap), dtype=torch.float32, device=self.device) for _ in range(2)]
+        rows = QROWS if self.quant else NROWS
+        new_state = [torch.zeros((rows, cap), dtype=torch.float32, device=self.device) for _ in range(2)]
         new_color = torch.zeros(cap, dtype=torch.int32, device=self.device)
         new_emit = torch.zeros(cap, dtype=torch.int32, device=self.device)
         if n > 0:
@@ -387,45 +395,62 @@ class MPMSolver:
 
     # ---------------------------------------------------------- seeding ---
 
-    def _append(self, x: torch.Tensor, material, color, velocity, emitter_id=0, E=None):
+    def _append(self, x: torch.Tensor, material, color, velocity, emitter_id=0, E=None, C=None, F=None, Jp=None):
         """Append particles with positions x (n,3) float32 on the device.
         engine/mpm_solver.py:823-838 (seed_particle): F = I, C = 0,
-        Jp = 0 for sand and 1 otherwise, v = source velocity."""
+        Jp = 0 for sand and 1 otherwise, v = source velocity.  C, F (n,3,3)
+        and Jp (n,) replace those defaults (exact checkpoints).  With
+        quant=True the rows are packed on the device (x, v and F rounded to
+        the stored formats)."""
         n = int(x.shape[0])
         if n == 0:
             return
         assert self.n_particles + n <= self.max_num_particles
         self._ensure_capacity(n)
-        s = self._state[self._cur]
-        si = s.view(torch.int32)
         a, b = self.n_particles, self.n_particles + n
-        s[ROW_X:ROW_X + 3, a:b] = x.t()
+        s = torch.empty((NROWS, n), dtype=torch.float32, device=self.device)
+        si = s.view(torch.int32)
+        s[ROW_X:ROW_X + 3] = x.t()
         if isinstance(velocity, torch.Tensor):
-            s[ROW_V:ROW_V + 3, a:b] = velocity.to(self.device, torch.float32).t()
+            s[ROW_V:ROW_V + 3] = velocity.to(self.device, torch.float32).t()
         else:
             self.set_source_velocity(velocity)
             vel = list(self.source_velocity)
             for d in range(3):
-                s[ROW_V + d, a:b] = float(np.float32(vel[d]))
-        s[ROW_C:ROW_C + 9, a:b] = 0.0
-        s[ROW_F:ROW_F + 9, a:b] = 0.0
+                s[ROW_V + d] = float(np.float32(vel[d]))
+        s[ROW_C:ROW_C + 9] = 0.0
+        s[ROW_F:ROW_F + 9] = 0.0
         for d in range(3):
-            s[ROW_F + 4 * d, a:b] = 1.0
+            s[ROW_F + 4 * d] = 1.0
         if isinstance(material, torch.Tensor):
             mat = material.to(self.device, torch.int32)
-            si[ROW_MAT, a:b] = mat
-            s[ROW_JP, a:b] = torch.where(mat == self.material_sand, 0.0, 1.0)
+            si[ROW_MAT] = mat
+            s[ROW_JP] = torch.where(mat == self.material_sand, 0.0, 1.0)
         else:
-            si[ROW_MAT, a:b] = int(material)
-            s[ROW_JP, a:b] = 0.0 if int(material) == self.material_sand else 1.0
-        si[ROW_ID, a:b] = torch.arange(a, b, dtype=torch.int32, device=self.device)
+            si[ROW_MAT] = int(material)
+            s[ROW_JP] = 0.0 if int(material) == self.material_sand else 1.0
+        si[ROW_ID] = torch.arange(a, b, dtype=torch.int32, device=self.device)
+        s[ROW_EP] = 0.0
         if self.per_particle_E:
             if E is None:
-                s[ROW_EP, a:b] = float(self.E)
+                s[ROW_EP] = float(self.E)
             elif isinstance(E, torch.Tensor):
-                s[ROW_EP, a:b] = E.to(self.device, torch.float32)
+                s[ROW_EP] = E.to(self.device, torch.float32)
             else:
-                s[ROW_EP, a:b] = float(E)
+                s[ROW_EP] = float(E)
+        if C is not None:
+            s[ROW_C:ROW_C + 9] = C.reshape(n, 9).t().to(self.device, torch.float32)
+        if F is not None:
+            s[ROW_F:ROW_F + 9] = F.reshape(n, 9).t().to(self.device, torch.float32)
+        if Jp is not None:
+            s[ROW_JP] = Jp.to(self.device, torch.float32)
+        st = self._state[self._cur]
+        if self.quant:
+            _lib.check(
+                self._lib.mpm_quant_pack(_ptr(s), n, n, _ptr(st), self._cap, a, None, self.stream),
+                "mpm_quant_pack")
+        else:
+            st[:, a:b] = s
         if isinstance(color, torch.Tensor):
             self._color[a:b] = color.to(self.device, torch.int32)
         else:
@@ -436,6 +461,8 @@ class MPMSolver:
         self._rebin()
 
     def _note_region(self, lo, hi):
+        if self.quant and any(not (-2.0 <= float(c) < 2.0) for c in list(lo) + list(hi)):
+            raise ValueError("quant=True stores positions as fixed point in [-2, 2)")
         self._cover(lo, hi)
 
     @staticmethod
@@ -565,7 +592,7 @@ class MPMSolver:
         """Grow the grid window if particles got close to its edge."""
         if self.n_particles == 0:
             return
-        x = self._state[self._cur][ROW_X:ROW_X + 3, :self.n_particles]
+        x = self._rows_f32()[ROW_X:ROW_X + 3, :self.n_particles]
         mn, mx = self._finite_bounds(x.t())
         reach = (max(self.all_time_max_velocity, 1.0) * frame_dt * 2.0)
         self._cover([a - reach for a in mn], [b + reach for b in mx])
@@ -748,22 +775,36 @@ class MPMSolver:
 
     # --------------------------------------------------------- readback ---
 
-    def _gather(self, row0: int, ncols: int) -> torch.Tensor:
+    def _rows_f32(self) -> torch.Tensor:
+        """The current particle state in the float32 row layout (slot order):
+        the state buffer itself, or with quant=True a decoded copy."""
+        st = self._state[self._cur]
+        if not self.quant:
+            return st
+        n = self.n_particles
+        out = torch.empty((NROWS, max(n, 1)), dtype=torch.float32, device=self.device)
+        _lib.check(self._lib.mpm_quant_unpack(_ptr(st), self._cap, 0, n, _ptr(out), out.shape[1], self.stream),
+                   "mpm_quant_unpack")
+        return out
+
+    def _gather(self, row0: int, ncols: int, rows: torch.Tensor | None = None) -> torch.Tensor:
         n = self.n_particles
         out = torch.empty((n, ncols), dtype=torch.float32, device=self.device)
         if n:
+            rows = self._rows_f32() if rows is None else rows
             _lib.check(
-                self._lib.mpm_gather_rows(_ptr(self._state[self._cur]), self._cap, n, row0, ncols, _ptr(out),
+                self._lib.mpm_gather_rows(_ptr(rows), rows.shape[1], n, row0, ncols, _ptr(out),
                                           self.stream), "mpm_gather_rows")
         return out
 
     def particle_info(self):
         """engine/mpm_solver.py:1172-1191: copies in original particle order."""
         n = self.n_particles
+        rows = self._rows_f32() if n else None
         data = {
-            'position': self._gather(ROW_X, 3).cpu().numpy(),
-            'velocity': self._gather(ROW_V, 3).cpu().numpy(),
-            'material': (self._gather(ROW_MAT, 1).view(torch.int32).reshape(n) & 0xFF).cpu().numpy(),
+            'position': self._gather(ROW_X, 3, rows).cpu().numpy(),
+            'velocity': self._gather(ROW_V, 3, rows).cpu().numpy(),
+            'material': (self._gather(ROW_MAT, 1, rows).view(torch.int32).reshape(n) & 0xFF).cpu().numpy(),
             'color': self._color[:n].cpu().numpy() if n else np.zeros(0, np.int32),
         }
         if self.use_emitter_id:
@@ -800,18 +841,15 @@ class MPMSolver:
         hi = x.max(0).values.tolist() if n else [0, 0, 0]
         if n:
             self._note_region(lo, hi)
-            self._append(x, st['material'], st['color'], st['v'])
-            s = self._state[self._cur]
-            s[ROW_C:ROW_C + 9, :n] = st['C'].reshape(n, 9).t().to(self.device)
-            s[ROW_F:ROW_F + 9, :n] = st['F'].reshape(n, 9).t().to(self.device)
-            s[ROW_JP, :n] = st['Jp'].to(self.device)
+            self._append(x, st['material'], st['color'], st['v'], C=st['C'], F=st['F'], Jp=st['Jp'])
         self.t = st.get('t', 0.0)
         self.total_substeps = st.get('total_substeps', 0)
 
     def tensors(self):
-        """Zero-copy views of the current (sorted) particle state rows."""
+        """Zero-copy views of the current (sorted) particle state rows; with
+        quant=True, views of a decoded float32 copy."""
         n = self.n_particles
-        s = self._state[self._cur]
+        s = self._rows_f32()
         return {
             'x': s[ROW_X:ROW_X + 3, :n],
             'v': s[ROW_V:ROW_V + 3, :n],

@@ -35,14 +35,14 @@ class ParticleIO:
         if n == 0:
             raise ValueError("no particles to write")
         lib, dev, s = solver._lib, solver.device, solver.stream
-        st = solver._state[solver._cur]
+        st = solver._rows_f32()
         keys = torch.empty(12, dtype=torch.int32, device=dev)
         ranges = torch.empty(12, dtype=torch.float32, device=dev)
         xv = torch.empty((n, 3), dtype=torch.int32, device=dev)
         rgb = torch.empty((n, 3), dtype=torch.uint8, device=dev)
-        _lib.check(lib.mpm_particle_ranges(st.data_ptr(), solver._cap, n, keys.data_ptr(), ranges.data_ptr(), s),
+        _lib.check(lib.mpm_particle_ranges(st.data_ptr(), st.shape[1], n, keys.data_ptr(), ranges.data_ptr(), s),
                    "mpm_particle_ranges")
-        _lib.check(lib.mpm_quantize_particles(st.data_ptr(), solver._cap, n, ranges.data_ptr(), xv.data_ptr(), s),
+        _lib.check(lib.mpm_quantize_particles(st.data_ptr(), st.shape[1], n, ranges.data_ptr(), xv.data_ptr(), s),
                    "mpm_quantize_particles")
         _lib.check(lib.mpm_unpack_colors(solver._color.data_ptr(), n, rgb.data_ptr(), s), "mpm_unpack_colors")
         return (ranges.cpu().numpy().reshape(2, 3, 2), xv.cpu().numpy().view(np.uint32), rgb.cpu().numpy())

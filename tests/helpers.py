@@ -17,7 +17,8 @@ def oracle_config(scene_or_solver, gravity=(0.0, -9.8, 0.0)):
             pp.append(d)
         return O.Config(res=s.res, size=s.size if hasattr(s, "size") else 1.0, gravity=tuple(s.gravity),
                         postprocess=pp, unbounded=s.unbounded, water_density=s.water_density,
-                        padding=s.padding, support_plasticity=getattr(s, "support_plasticity", True))
+                        padding=s.padding, support_plasticity=getattr(s, "support_plasticity", True),
+                        quant=bool(getattr(s, "quant", False)))
     pp = [dict(kind=O.KIND_BOX, surface=0)] + list(s.postprocess)
     return O.Config(res=s.res, size=s.size, gravity=gravity, postprocess=pp, E_scale=getattr(s, "E_scale", 1.0))
 

@@ -119,5 +119,4 @@ def test_unsupported_flags_raise():
     from taichi_elements_gb300.mpm_solver import MPMSolver
     with pytest.raises(NotImplementedError):
         MPMSolver((16, 16))
-    with pytest.raises(NotImplementedError):
-        MPMSolver((16, 16, 16), quant=True)
+

@@ -41,6 +41,9 @@ P2G_BYTES_PER_NODE = 16
 G2P_BYTES_PER_PARTICLE = 60  # write x, v, C
 G2P_BYTES_PER_NODE = 16
 GRID_BYTES_PER_NODE = 32
+# packed storage (quant=True): x 8, v 8, F with the material 20, C 36, Jp 4
+Q_ALGO_BYTES_PER_PARTICLE = 152  # read 76 + write x, v, C, F, Jp 76
+Q_P2G_BYTES_PER_PARTICLE = 100  # read 76 + write F, Jp 24
 KERNELS_PER_SUBSTEP = 9  # 6 binning kernels + p2g + grid + g2p
 
 
@@ -195,7 +198,8 @@ def run_gb300(args):
 
     ws, rank, local = dist_init()
     sc = make_scene(args.workload)
-    solver = sc.make_solver(chunk=args.chunk) if args.chunk else sc.make_solver()
+    skw = dict(quant=True) if args.quant else {}
+    solver = sc.make_solver(chunk=args.chunk, **skw) if args.chunk else sc.make_solver(**skw)
     dt = sc.default_dt
     chunk_times = None
     if not args.chunk:
@@ -256,12 +260,14 @@ def run_gb300(args):
     n = solver.n_particles
     value = replica_value(n, args.steps, ws, total_ms)
     peak, peak_kind = load_peaks()
-    p2g_bytes = P2G_BYTES_PER_PARTICLE * n + P2G_BYTES_PER_NODE * n_nodes
+    per_p2g = Q_P2G_BYTES_PER_PARTICLE if args.quant else P2G_BYTES_PER_PARTICLE
+    per_sub = Q_ALGO_BYTES_PER_PARTICLE if args.quant else ALGO_BYTES_PER_PARTICLE
+    p2g_bytes = per_p2g * n + P2G_BYTES_PER_NODE * n_nodes
     p2g_ach = p2g_bytes / (ph_mean[1] / 1e3) / 1e9
-    sub_bytes = ALGO_BYTES_PER_PARTICLE * n + ALGO_BYTES_PER_NODE * n_nodes
+    sub_bytes = per_sub * n + ALGO_BYTES_PER_NODE * n_nodes
     sub_ach = sub_bytes / ((ph_mean[1] + ph_mean[2] + ph_mean[3]) / 1e3) / 1e9
     full_ach = sub_bytes / (ph.sum(1).mean() / 1e3) / 1e9
-    traffic = p2g_traffic(n)
+    traffic = None if args.quant else p2g_traffic(n)
 
     e2e = None
     if not args.no_e2e:
@@ -278,6 +284,9 @@ def run_gb300(args):
     g2p2g = None
     if not args.no_g2p2g:
         g2p2g = run_g2p2g_measure(sc)
+    quant = None
+    if not args.no_quant:
+        quant = run_quant_measure(sc)
     pio = mesh = None
     if not args.no_io:
         pio = run_particle_output_measure(solver, peak, peak_kind, rank == 0 and not args.no_cpu)
@@ -299,7 +308,7 @@ def run_gb300(args):
         "dtype": "f32",
         "data": "synthetic (seeded numpy scene generator; no dataset)",
         "config": {
-            "workload": f"{sc.name}: {describe(sc)}",
+            "workload": f"{sc.name}: {describe(sc)}" + (", packed particle storage (quant=True)" if args.quant else ""),
             "particles": n,
             "grid": list(sc.res),
             "grid_nodes_touched": n_nodes,
@@ -324,6 +333,7 @@ def run_gb300(args):
         "batched": batched,
         "fwd_adjoint": adjoint,
         "g2p2g": g2p2g,
+        "quant": quant,
         "render": render,
         "particle_output": pio,
         "mesh_emitter": mesh,
@@ -488,6 +498,48 @@ def run_mesh_emitter_measure(peak, peak_kind, with_cpu, reps=5):
         out["cpu_baseline"] = {"value": len(sample) / tc, "unit": "triangles/s", "cores": 1, "kind": "port",
                                "sample": f"{len(sample)} of the triangles through the numpy restatement of "
                                          "Voxelizer.voxelize_triangles on the same 512^3 voxel grid"}
+    return out
+
+
+def run_mode_measure(sc, substeps=50, warmup=5, **solver_kw):
+    """The same scene with other solver modes (use_g2p2g, quant,
+    support_plasticity): K substeps timed with CUDA events; returns
+    (ms per substep, particles)."""
+    import torch
+    s = sc.make_solver(chunk=512, **solver_kw)
+    dt = sc.default_dt
+    s._prepare(dt)
+    for _ in range(warmup):
+        s._launch_substep(dt, -1)
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(substeps):
+        s._launch_substep(dt, -1)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / substeps
+    if int(s._status.item()):
+        raise RuntimeError(f"device status set during the {solver_kw} measurement")
+    n = s.n_particles
+    rows = int(s._state[0].shape[0])
+    del s
+    torch.cuda.empty_cache()
+    return ms, n, rows
+
+
+def run_quant_measure(sc, substeps=50):
+    """quant=True (engine/mpm_solver.py:106-127, :216-262): the packed
+    particle layout in the plain substep and in the fused G2P2G mode with
+    support_plasticity=False (the reference's quantized demos)."""
+    out = {"unit": "particle-substeps/s", "substeps": substeps}
+    for key, kw in (("plain", dict(quant=True)),
+                    ("g2p2g_no_plasticity", dict(quant=True, use_g2p2g=True, support_plasticity=False))):
+        ms, n, rows = run_mode_measure(sc, substeps, **kw)
+        out[key] = {"value": n / (ms / 1e3), "ms_per_substep": ms}
+        out["state_bytes_per_particle"] = 4 * rows
+    out["float32_state_bytes_per_particle"] = 4 * 28
     return out
 
 
@@ -755,6 +807,9 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-io", action="store_true", help="skip the particle-output and mesh-emitter measurements")
     ap.add_argument("--no-g2p2g", action="store_true", help="skip the fused G2P2G-mode measurement")
+    ap.add_argument("--no-quant", action="store_true", help="skip the packed-storage (quant=True) measurement")
+    ap.add_argument("--quant", action="store_true",
+                    help="run the timed substeps with packed particle storage (quant=True)")
     ap.add_argument("--no-render", action="store_true", help="skip the path-tracer measurement")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--e2e-frames", type=int, default=3)

@@ -67,3 +67,26 @@ def test_write_particles_ply_original_order(tmp_path):
     info = s.particle_info()
     np.testing.assert_array_equal(rows[:, :3], info["position"])
     np.testing.assert_array_equal(rows[:, 3].view(np.int32), info["color"])
+
+
+def test_blender_cache_frame_round_trip(tmp_path):
+    """blender/operators.py:228-247 for a GB300 solver: the five attribute
+    files hold particle_info's arrays in original order, and the header is
+    the reference's format (checked against its own bytes on the CPU)."""
+    from taichi_elements_gb300 import blender_cache as B
+    from taichi_elements_gb300.mpm_solver import MPMSolver
+    s = MPMSolver((32, 32, 32), use_emitter_id=True)
+    s.add_cube((0.3, 0.3, 0.3), (0.2, 0.2, 0.2), MPMSolver.material_snow, color=0x123456)
+    s.add_ellipsoid((0.6, 0.6, 0.6), 0.1, MPMSolver.material_water, color=0xABCDEF, velocity=(1, 0, 0))
+    for _ in range(3):
+        s.step(4e-3)
+    path = B.save_particles(s, str(tmp_path), 17)
+    assert os.path.basename(path) == 'particles_000017.bin'
+    out = B.read_pars(path)
+    info = s.particle_info()
+    n = info['position'].shape[0]
+    np.testing.assert_array_equal(out[B.POS].reshape(n, 3), info['position'])
+    np.testing.assert_array_equal(out[B.VEL].reshape(n, 3), info['velocity'])
+    np.testing.assert_array_equal(out[B.COL], info['color'])
+    np.testing.assert_array_equal(out[B.MAT], info['material'])
+    np.testing.assert_array_equal(out[B.EMT], info['emitter_ids'])

@@ -51,6 +51,17 @@ def _ptr(t: torch.Tensor) -> int:
     return t.data_ptr()
 
 
+class ParticleCount(int):
+    """The particle count: an int that also reads like the reference's
+    scalar field, ``solver.n_particles[None]`` (engine/mpm_solver.py:88,
+    used by demo/demo_3d_bunnies_recursive.py:136)."""
+
+    def __getitem__(self, key):
+        if key is None or key == ():
+            return int(self)
+        raise TypeError("n_particles is a scalar: index it with [None]")
+
+
 class MPMSolver:
     material_water = 0
     material_elastic = 1
@@ -306,6 +317,23 @@ class MPMSolver:
     def add_bounding_box(self, unbounded):
         self.grid_postprocess.append(dict(kind=KIND_BOX, surface=int(bool(unbounded))))
         self._invalidate_params()
+
+    @property
+    def n_particles(self) -> ParticleCount:
+        return ParticleCount(self._n)
+
+    @n_particles.setter
+    def n_particles(self, value):
+        self._n = int(value)
+
+    @property
+    def particle(self):
+        """Per-particle storage size in the form of the reference's particle
+        SNode (demo/demo_3d_bunnies_recursive.py:151 prints
+        ``particle._cell_size_bytes``): state rows plus colour and emitter id."""
+        import types
+        rows = QROWS if self.quant else NROWS
+        return types.SimpleNamespace(_cell_size_bytes=4 * rows + 8)
 
     # ------------------------------------------------------ allocation ---
 

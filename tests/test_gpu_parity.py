@@ -191,6 +191,9 @@ def test_particle_info_original_order_and_fields():
     np.testing.assert_array_equal(info2['color'], color)
     # particles stay near where they were: the readback is in original order
     assert np.abs(info2['position'] - sc.x).max() < 0.05
+    # the reference's scalar-field reads and per-particle size keep working
+    assert s.n_particles[None] == sc.n and s.n_particles == sc.n
+    assert s.particle._cell_size_bytes == 4 * 28 + 8
 
 
 def test_seeding_counts_match_reference_rules():

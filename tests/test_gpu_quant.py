@@ -10,7 +10,7 @@
   fields can differ where float32 rounding noise crosses a rounding
   boundary of the packed format: at most one unit of the format (x: 2^-19,
   F: 4.1 / 2^15, v: one mantissa unit, 2^-17 of the largest component,
-  plus 1e-6 of the largest velocity for the float32 noise of the gather),
+  plus the plain substep's 1e-5 of the largest velocity),
   on under 1% of the particles for x and 5% for F (v's unit sits close to
   float32 noise, so only the bound applies to it).
 """
@@ -110,12 +110,13 @@ def _check_fields(s, P, v_tol_rel=2.0**-17):
     ex, fx = _field_errors(x, P.x, X_UNIT)
     eF, fF = _field_errors(F, P.F, F_UNIT)
     # v: one mantissa unit of the particle's largest component on top of the
-    # float32 noise of the gather (1e-6 of the largest velocity)
+    # plain substep's bound for v (1e-5 of the largest velocity: float32
+    # atomics reorder the grid sums)
     dv = np.abs(v - P.v).max(1) - v_tol_rel * np.abs(P.v).max(1)
     ev = dv.max() / np.abs(P.v).max()
     assert ex <= 1.0001 and fx < 0.01, (ex, fx)
     assert eF <= 1.01 and fF < 0.05, (eF, fF)  # one unit up to float32 rounding of q * scale
-    assert ev <= 1e-6, ev
+    assert ev <= 1e-5, ev
 
 
 @pytest.mark.parametrize("plasticity", [True, False])

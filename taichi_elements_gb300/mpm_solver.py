@@ -620,8 +620,7 @@ class MPMSolver:
         """Grow the grid window if particles got close to its edge."""
         if self.n_particles == 0:
             return
-        x = self._rows_f32()[ROW_X:ROW_X + 3, :self.n_particles]
-        mn, mx = self._finite_bounds(x.t())
+        mn, mx = self._finite_bounds(self._positions_f32())
         reach = (max(self.all_time_max_velocity, 1.0) * frame_dt * 2.0)
         self._cover([a - reach for a in mn], [b + reach for b in mx])
         if self._ws is None:
@@ -813,6 +812,23 @@ class MPMSolver:
         out = torch.empty((NROWS, max(n, 1)), dtype=torch.float32, device=self.device)
         _lib.check(self._lib.mpm_quant_unpack(_ptr(st), self._cap, 0, n, _ptr(out), out.shape[1], self.stream),
                    "mpm_quant_unpack")
+        return out
+
+    def _positions_f32(self) -> torch.Tensor:
+        """Positions (3, n) as float32 in slot order; with quant=True decoded
+        from the packed word pair (three 21-bit fields of scale 2^-19) by
+        torch integer ops, without decoding the other rows."""
+        n = self.n_particles
+        st = self._state[self._cur]
+        if not self.quant:
+            return st[ROW_X:ROW_X + 3, :n].t()
+        w = st[0:2, :n].view(torch.int32).to(torch.int64) & 0xFFFFFFFF
+        w = w[0] | (w[1] << 32)
+        out = torch.empty((n, 3), dtype=torch.float32, device=self.device)
+        for d in range(3):
+            q = (w >> (21 * d)) & 0x1FFFFF
+            q = q - ((q >> 20) << 21)  # sign-extend 21 bits
+            out[:, d] = q.to(torch.float32) * (1.0 / 524288.0)
         return out
 
     def _gather(self, row0: int, ncols: int, rows: torch.Tensor | None = None) -> torch.Tensor:

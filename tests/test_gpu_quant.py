@@ -75,6 +75,8 @@ def test_seeding_stores_packed_values():
     info = s.particle_info()
     np.testing.assert_array_equal(info['position'], xq)
     assert s._state[0].shape[0] == _lib.QROWS
+    # the position-only decode of the window checks equals the full decode
+    torch.testing.assert_close(s._positions_f32(), s._rows_f32()[0:3, :n].t(), rtol=0, atol=0)
     with pytest.raises(ValueError):
         s.add_cube((1.9, 0.5, 0.5), (0.2, 0.1, 0.1), 0)
 

@@ -16,7 +16,7 @@ def test_growth_keeps_particles(quant):
     s = MPMSolver((64, 64, 64), quant=quant, seed=3)
     caps = []
     before = None
-    # 16,777 + 56,623 + 89,915 + 56,623 particles: capacity 65,536 -> 131,072 -> 262,144
+    # 16,778 + 56,624 + 89,916 + 56,624 particles: capacity 65,536 -> 131,072 -> 262,144
     for k, (lo, side, mat) in enumerate([((0.1, 0.1, 0.1), 0.2, 1), ((0.5, 0.1, 0.5), 0.3, 0), ((0.1, 0.5, 0.1), 0.35, 2),
                                          ((0.55, 0.55, 0.55), 0.3, 3)]):
         if before is not None:

@@ -37,7 +37,11 @@ struct Ws {
   int32_t *lvl_L;                // [cap]
   int2 *items;                   // [cap/32 + nblk + 1]
   int32_t *cellkey, *pid;  // [cap]
+  int32_t *slot_rank;  // [cap] rank inside its cell of the particle at sorted slot j
+  int32_t *stay_rank;  // [cap] next rank of a particle that stays in its cell, else -1
   int32_t *cell_cnt;              // [nblk * 64]
+  int32_t *arr_cnt, *arr_rank;    // [nblk * 64] particles without a kept rank: count, next rank
+  unsigned long long *leave;      // [nblk * 64] ranks (< 64) of the particles that left the cell
   float4 *grid_mom;               // [nblk * 64] (m, mv)
   float4 *grid_vel;               // [nblk * 64] (v, m)
   int64_t nblk;
@@ -77,7 +81,12 @@ inline size_t ws_layout(const MpmParams &p, int64_t cap, char *base, Ws *w) {
   t.items = (int2 *)take((size_t)items_cap * 8);
   t.cellkey = (int32_t *)take((size_t)cap * 4);
   t.pid = (int32_t *)take((size_t)cap * 4);
+  t.slot_rank = (int32_t *)take((size_t)cap * 4);
+  t.stay_rank = (int32_t *)take((size_t)cap * 4);
   t.cell_cnt = (int32_t *)take((size_t)nblk * kBlockCells * 4);
+  t.arr_cnt = (int32_t *)take((size_t)nblk * kBlockCells * 4);
+  t.arr_rank = (int32_t *)take((size_t)nblk * kBlockCells * 4);
+  t.leave = (unsigned long long *)take((size_t)nblk * kBlockCells * 8);
   t.grid_mom = (float4 *)take((size_t)nblk * kBlockCells * 16);
   t.grid_vel = (float4 *)take((size_t)nblk * kBlockCells * 16);
   t.nblk = nblk;

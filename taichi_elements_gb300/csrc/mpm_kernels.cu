@@ -9,19 +9,24 @@
 //   k_pb_stats/k_pb_scan          per particle block: count, start, level
 //                                 table base and work-item base (two-pass scan)
 //   k_pb_levels                   rank-major level tables, work items, clears
-//                                 the cell counters and block flags
+//                                 the block flags
 //   k_scatter                     sorted order pid[pos] = i
+//   k_cell_clear                  clears the cell counters
 //   k_p2g                         per work item: stress, APIC scatter into a
 //                                 shared-memory 6^3 tile, one float4 atomic
 //                                 flush per touched node
 //   k_grid                        momentum->velocity, gravity, box, colliders
 //   k_g2p                         per work item: 6^3 velocity tile in shared
-//                                 memory, gather, advect, bin for next substep
+//                                 memory, gather, advect, bin for the next
+//                                 substep
 //
 // Sorted order inside a block is rank-major: all cells' first particles (in
 // cell order), then all cells' second particles, ...  Consecutive lanes thus
 // work on different cells, so their shared-memory atomics and gathers hit
-// different nodes, while global loads stay coalesced.
+// different nodes.  A particle that stays in its cell keeps its rank (less
+// the cell's leavers ranked below it), so the sorted order changes only
+// where particles cross cells and P2G's reads of the previous order through
+// pid stay nearly contiguous.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -78,12 +83,20 @@ __device__ __forceinline__ const MpmParams &scene_of_block(const MpmParams &P, c
   }
 }
 
+// Bins the particle at slot i for the next substep and returns its cell key.
+// A particle still in cell old_key with a rank r_old < 64 there keeps that
+// rank, less the cell's leavers ranked below it (k_scatter subtracts them);
+// the others get their rank from the arrival order in k_scatter.
 template <bool BATCH>
-__device__ __forceinline__ void bin_one(const MpmParams &P, const MpmParams *tab, const Ws &w, int64_t i, float x0,
-                                        float x1, float x2, int matword, uint32_t &bad) {
+__device__ __forceinline__ int bin_one(const MpmParams &P, const MpmParams *tab, const Ws &w, int64_t i, float x0,
+                                       float x1, float x2, int matword, uint32_t &bad, int old_key = -1,
+                                       int r_old = -1) {
   const Base b = particle_base(scene_of_particle<BATCH>(P, tab, matword), x0, x1, x2, bad);
   const int key = cell_key(P, b);
-  atomicAdd(&w.cell_cnt[key], 1);  // result unused: a fire-and-forget reduction
+  const int sr = (key == old_key && (unsigned)r_old < 64u) ? r_old : -1;
+  atomicAdd(&w.cell_cnt[key], 1);  // results unused: fire-and-forget reductions
+  if (sr < 0) atomicAdd(&w.arr_cnt[key], 1);
+  w.stay_rank[i] = sr;
   const int blin = key >> 6;
   // Blocks this particle's 3^3 stencil reaches: its own block plus, per axis,
   // the next block when the base sits in the last two cells of the block.
@@ -98,6 +111,7 @@ __device__ __forceinline__ void bin_one(const MpmParams &P, const MpmParams *tab
   const int all = (int)__reduce_or_sync(same, (unsigned)mask);
   if ((threadIdx.x & 31) == __ffs(same) - 1) atomicOr(&w.blk_flag[blin], all);
   w.cellkey[i] = key;
+  return key;
 }
 
 template <bool BATCH, bool Q>
@@ -287,7 +301,8 @@ __global__ __launch_bounds__(256) void k_pb_scan(const MpmParams P, const Ws w) 
 }
 
 // One warp per particle block: rank-major level table, work items, and the
-// clearing of the cell counters and the block flag.
+// clearing of the block flag (the cell counters are cleared by k_cell_clear
+// once k_scatter has ranked the particles).
 __global__ __launch_bounds__(256) void k_pb_levels(const MpmParams P, const Ws w, int64_t cap) {
   const int npb = w.counters[0];
   const int lane = threadIdx.x & 31;
@@ -322,7 +337,6 @@ __global__ __launch_bounds__(256) void k_pb_levels(const MpmParams P, const Ws w
       else
         set_status(w, MPM_STATUS_TABLE_OVERFLOW);
     }
-    // the cell counters are counted back to zero by k_scatter
     if (lane == 0) w.blk_flag[blin] = 0;
   }
 }
@@ -331,12 +345,16 @@ __global__ void k_scatter(const MpmParams P, const Ws w, int64_t n) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int key = w.cellkey[i];
-  // rank inside the cell: count the cell's counter back down (this also
-  // leaves it zero for the next binning pass)
-  const int r = atomicSub(&w.cell_cnt[key], 1) - 1;
+  // Rank inside the cell: particles that stayed in their cell keep their
+  // order (ranks 0 .. N - A - 1, set in G2P); the A others take the ranks
+  // above in arrival order.
+  const int sr = w.stay_rank[i];
+  const int N = w.cell_cnt[key];
+  const int r = sr >= 0 ? sr - __popcll(w.leave[key] & ((1ull << sr) - 1ull))
+                        : (N - w.arr_cnt[key]) + atomicAdd(&w.arr_rank[key], 1);
   const int blin = key >> 6, c = key & 63;
   const int k = w.blk_slot[blin];
-  if (k < 0 || k >= w.counters[0] || r < 0) {  // stale binning: report, never index out of range
+  if (k < 0 || k >= w.counters[0] || r < 0 || r >= N) {  // stale binning: report, never index out of range
     set_status(w, MPM_STATUS_TABLE_OVERFLOW);
     return;
   }
@@ -352,6 +370,26 @@ __global__ void k_scatter(const MpmParams P, const Ws w, int64_t n) {
     return;
   }
   w.pid[pos] = (int)i;
+  w.slot_rank[pos] = r;
+}
+
+// Clears the per-cell counters and leave masks of the particle blocks once
+// k_scatter has used them, ready for the next binning.  The next G2P marks
+// leavers only in cells of these blocks (their cells before advection), and
+// k_scatter reads a mask only at a stayer's cell, which was a cell of the
+// previous particle blocks too: masks left in blocks that emptied are never
+// read before their block is cleared again.
+__global__ __launch_bounds__(256) void k_cell_clear(const MpmParams P, const Ws w) {
+  const int npb = w.counters[0];
+  const int64_t total = (int64_t)npb * kBlockCells;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t a = (int64_t)w.pblocks[t >> 6] * kBlockCells + (t & 63);
+    w.cell_cnt[a] = 0;
+    w.arr_cnt[a] = 0;
+    w.arr_rank[a] = 0;
+    w.leave[a] = 0ull;
+  }
 }
 
 // ---------------------------------------------------------------- P2G ----
@@ -529,7 +567,10 @@ __global__ __launch_bounds__(256) void k_grid(const MpmParams P, const MpmParams
 
 // ---------------------------------------------------------------- G2P ----
 
-template <bool BATCH, bool Q>
+// KEEP: particles that stay in their cell keep their rank there (bin_one
+// with the old key and rank; a particle that leaves marks its old rank in
+// the old cell's leave mask, which k_scatter subtracts from the stayers').
+template <bool BATCH, bool Q, bool KEEP>
 __global__ __launch_bounds__(kG2PThreads, 8) void k_g2p(const MpmParams P, const MpmParams *tab, const Ws w,
                                                        float *__restrict__ st, int64_t cap, float dt,
                                                        float *maxv_out) {
@@ -621,7 +662,14 @@ __global__ __launch_bounds__(kG2PThreads, 8) void k_g2p(const MpmParams P, const
         ld_v<Q>(st, cap, j, vv);
       }
       vmax = fmaxf(vmax, fmaxf(fabsf(vv[0]), fmaxf(fabsf(vv[1]), fabsf(vv[2]))));
-      bin_one<BATCH>(P, tab, w, j, x[0], x[1], x[2], matword, bad);  // next substep's build_pid
+      if (KEEP) {  // next substep's build_pid, keeping the rank of a stayer
+        const int old_key = cell_key(P, b);
+        const int r_old = w.slot_rank[j];
+        const int key = bin_one<BATCH>(P, tab, w, j, x[0], x[1], x[2], matword, bad, old_key, r_old);
+        if (key != old_key && (unsigned)r_old < 64u) atomicOr(&w.leave[old_key], 1ull << r_old);
+      } else {
+        bin_one<BATCH>(P, tab, w, j, x[0], x[1], x[2], matword, bad);  // next substep's build_pid
+      }
     }
     if (BATCH && maxv_out) {  // per-scene maximum, flushed per work item
 #pragma unroll
@@ -906,15 +954,15 @@ static const DevInfo *dev_info() {
     int a = 0, b = 0, c = 0, a2 = 0, b2 = 0, c2 = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_p2g<false, false, false>, kP2GThreads, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_p2g<true, false, false>, kP2GThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_g2p<false, false>, kG2PThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_g2p<false, false, true>, kG2PThreads, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a2, k_p2g<false, true, false>, kP2GThreads, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_p2g<true, true, false>, kP2GThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c2, k_g2p<true, false>, kG2PThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c2, k_g2p<true, false, false>, kG2PThreads, 0);
     int f = 0, aq = 0, bq = 0, cq = 0, fq = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, k_g2p2g<false>, kP2GThreads, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&aq, k_p2g<false, false, true>, kP2GThreads, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bq, k_p2g<true, false, true>, kP2GThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cq, k_g2p<false, true>, kG2PThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cq, k_g2p<false, true, true>, kG2PThreads, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fq, k_g2p2g<true>, kP2GThreads, 0);
     d.g2p2g_ctas = sms * (f > 0 ? f : 1);
     d.p2g_q_ctas = sms * (aq > 0 ? aq : 1);
@@ -1025,6 +1073,7 @@ int mpm_bin_finalize(const MpmParams *p, void *ws, int64_t cap, int64_t n, void 
   k_pb_scan<<<w.nstattiles, 256, 0, s>>>(*p, w);
   k_pb_levels<<<di->sms * 8, 256, 0, s>>>(*p, w, cap);
   if (n > 0) k_scatter<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(*p, w, n);
+  k_cell_clear<<<di->sms * 8, 256, 0, s>>>(*p, w);
   return last_error();
 }
 
@@ -1067,10 +1116,10 @@ int mpm_g2p(const MpmParams *p, void *ws, int64_t cap, int64_t n, float *nxt, fl
   Ws w;
   ws_layout(*p, cap, (char *)ws, &w);
   if (p->quant)
-    k_g2p<false, true><<<di->g2p_q_ctas, kG2PThreads, 0, (cudaStream_t)stream>>>(*p, nullptr, w, nxt, cap, dt,
+    k_g2p<false, true, true><<<di->g2p_q_ctas, kG2PThreads, 0, (cudaStream_t)stream>>>(*p, nullptr, w, nxt, cap, dt,
                                                                                  maxv_out);
   else
-    k_g2p<false, false><<<di->g2p_ctas, kG2PThreads, 0, (cudaStream_t)stream>>>(*p, nullptr, w, nxt, cap, dt,
+    k_g2p<false, false, true><<<di->g2p_ctas, kG2PThreads, 0, (cudaStream_t)stream>>>(*p, nullptr, w, nxt, cap, dt,
                                                                                 maxv_out);
   return last_error();
 }
@@ -1084,11 +1133,15 @@ int mpm_g2p_bin_into(const MpmParams *p, void *ws, void *ws_bins, int64_t cap, i
   ws_layout(*p, cap, (char *)ws, &w);
   ws_layout(*p, cap, (char *)ws_bins, &wb);
   // the grid, sorted order and status stay with `ws`; only the next
-  // substep's cell counts, block flags and cell keys go to `ws_bins`
+  // substep's cell counts, block flags, cell keys and rank records go to
+  // `ws_bins`
   w.cell_cnt = wb.cell_cnt;
   w.blk_flag = wb.blk_flag;
   w.cellkey = wb.cellkey;
-  k_g2p<false, false><<<di->g2p_ctas, kG2PThreads, 0, (cudaStream_t)stream>>>(*p, nullptr, w, nxt, cap, dt, maxv_out);
+  w.stay_rank = wb.stay_rank;
+  w.arr_cnt = wb.arr_cnt;
+  k_g2p<false, false, false><<<di->g2p_ctas, kG2PThreads, 0, (cudaStream_t)stream>>>(*p, nullptr, w, nxt, cap, dt,
+                                                                                     maxv_out);
   return last_error();
 }
 
@@ -1167,7 +1220,7 @@ int mpm_batch_substep(const MpmParams *p, const MpmParams *scenes, void *ws, int
   else
     k_p2g<false, true, false><<<di->p2g_b_ctas, kP2GThreads, 0, s>>>(*p, scenes, w, cur, nxt, cap, 0.0f);
   k_grid<true><<<di->sms * 8, 256, 0, s>>>(*p, scenes, w, 0.0f);
-  k_g2p<true, false><<<di->g2p_b_ctas, kG2PThreads, 0, s>>>(*p, scenes, w, nxt, cap, 0.0f, maxv_out);
+  k_g2p<true, false, false><<<di->g2p_b_ctas, kG2PThreads, 0, s>>>(*p, scenes, w, nxt, cap, 0.0f, maxv_out);
   return last_error();
 }
 
@@ -1196,12 +1249,13 @@ int mpm_substep_noalloc(const MpmParams *p, int64_t cap, int64_t n, const float 
     k_pb_scan<<<w.nstattiles, 256, 0, s>>>(*p, w);
     k_pb_levels<<<di->sms * 8, 256, 0, s>>>(*p, w, kStaticMaxParticles);
     k_scatter<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(*p, w, n);
+    k_cell_clear<<<di->sms * 8, 256, 0, s>>>(*p, w);
     if (p->has_Ep)
       k_p2g<true, false, false><<<di->p2g_ep_ctas, kP2GThreads, 0, s>>>(*p, nullptr, w, cur, nxt, cap, dt);
     else
       k_p2g<false, false, false><<<di->p2g_ctas, kP2GThreads, 0, s>>>(*p, nullptr, w, cur, nxt, cap, dt);
     k_grid<false><<<di->sms * 8, 256, 0, s>>>(*p, nullptr, w, dt);
-    k_g2p<false, false><<<di->g2p_ctas, kG2PThreads, 0, s>>>(*p, nullptr, w, nxt, cap, dt, maxv_out);
+    k_g2p<false, false, false><<<di->g2p_ctas, kG2PThreads, 0, s>>>(*p, nullptr, w, nxt, cap, dt, maxv_out);
   }
   return last_error();
 }

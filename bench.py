@@ -44,7 +44,7 @@ GRID_BYTES_PER_NODE = 32
 # packed storage (quant=True): x 8, v 8, F with the material 20, C 36, Jp 4
 Q_ALGO_BYTES_PER_PARTICLE = 152  # read 76 + write x, v, C, F, Jp 76
 Q_P2G_BYTES_PER_PARTICLE = 100  # read 76 + write F, Jp 24
-KERNELS_PER_SUBSTEP = 9  # 6 binning kernels + p2g + grid + g2p
+KERNELS_PER_SUBSTEP = 10  # 7 binning kernels + p2g + grid + g2p
 
 
 def load_peaks():
@@ -565,7 +565,7 @@ def run_g2p2g_measure(sc, substeps=50, warmup=5):
         raise RuntimeError("device status set during the G2P2G measurement")
     n = s.n_particles
     out = {"value": n / (ms / 1e3), "unit": "particle-substeps/s (fused G2P2G mode)", "ms_per_substep": ms,
-           "substeps": substeps, "gpu_launches_per_substep": 8,
+           "substeps": substeps, "gpu_launches_per_substep": 9,
            "note": "use_g2p2g=True semantics (reference :363-485): C not stored, p_mass for every material"}
     del s
     torch.cuda.empty_cache()

@@ -7,7 +7,7 @@ its own slot of one shared grid window: binning, block lists and grids are
 shared, each particle carries its scene index in bits 8.. of its material
 word, and the kernels read the scene's constants (dx, dt, Young's modulus,
 gravity, bounding box, colliders) from a device table of per-scene
-``MpmParams`` rows.  One substep of all scenes is one set of 9 launches;
+``MpmParams`` rows.  One substep of all scenes is one set of 10 launches;
 frames of substeps are captured in a CUDA graph.
 """
 from __future__ import annotations

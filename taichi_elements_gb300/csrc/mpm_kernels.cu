@@ -830,7 +830,12 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_g2p2g(const M
           } else {
             cell = (tx0 * kFusedTileW + ty0) * kFusedTileW + tz0;
           }
-          bin_one<false>(P, nullptr, w, j, x[0], x[1], x[2], matword, bad);  // next substep's build_pid
+          {  // next substep's build_pid, keeping the rank of a stayer (as in k_g2p)
+            const int old_key = cell_key(P, b);
+            const int r_old = w.slot_rank[j];
+            const int key = bin_one<false>(P, nullptr, w, j, x[0], x[1], x[2], matword, bad, old_key, r_old);
+            if (key != old_key && (unsigned)r_old < 64u) atomicOr(&w.leave[old_key], 1ull << r_old);
+          }
         }
       }
       if (active && direct) {  // rare: straight to the grid

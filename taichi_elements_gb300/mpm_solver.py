@@ -842,18 +842,35 @@ class MPMSolver:
         return out
 
     def particle_info(self):
-        """engine/mpm_solver.py:1172-1191: copies in original particle order."""
+        """engine/mpm_solver.py:1172-1191: copies in original particle order.
+
+        The arrays are gathered on the device and copied into page-locked
+        host memory (PyTorch's caching host allocator, so repeated frames
+        reuse it) with one synchronisation for all of them; each returned
+        numpy array owns its buffer like the reference's fresh copies."""
         n = self.n_particles
-        rows = self._rows_f32() if n else None
-        data = {
-            'position': self._gather(ROW_X, 3, rows).cpu().numpy(),
-            'velocity': self._gather(ROW_V, 3, rows).cpu().numpy(),
-            'material': (self._gather(ROW_MAT, 1, rows).view(torch.int32).reshape(n) & 0xFF).cpu().numpy(),
-            'color': self._color[:n].cpu().numpy() if n else np.zeros(0, np.int32),
+        if n == 0:
+            data = {'position': np.zeros((0, 3), np.float32), 'velocity': np.zeros((0, 3), np.float32),
+                    'material': np.zeros(0, np.int32), 'color': np.zeros(0, np.int32)}
+            if self.use_emitter_id:
+                data['emitter_ids'] = np.zeros(0, np.int32)
+            return data
+        rows = self._rows_f32()
+        dev = {
+            'position': self._gather(ROW_X, 3, rows),
+            'velocity': self._gather(ROW_V, 3, rows),
+            'material': self._gather(ROW_MAT, 1, rows).view(torch.int32).reshape(n) & 0xFF,
+            'color': self._color[:n],
         }
         if self.use_emitter_id:
-            data['emitter_ids'] = self._emitter[:n].cpu().numpy() if n else np.zeros(0, np.int32)
-        return data
+            dev['emitter_ids'] = self._emitter[:n]
+        host = {}
+        for k, t in dev.items():
+            h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+            h.copy_(t, non_blocking=True)
+            host[k] = h
+        torch.cuda.current_stream(self.device).synchronize()
+        return {k: h.numpy() for k, h in host.items()}
 
     def full_state(self):
         """All particle fields in original order as float32 device tensors:

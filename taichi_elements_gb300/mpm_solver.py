@@ -864,13 +864,19 @@ class MPMSolver:
         }
         if self.use_emitter_id:
             dev['emitter_ids'] = self._emitter[:n]
-        host = {}
-        for k, t in dev.items():
+        return dict(zip(dev.keys(), self._to_host(*dev.values())))
+
+    def _to_host(self, *tensors):
+        """numpy copies of device tensors through page-locked buffers (the
+        caching host allocator reuses them across frames), one
+        synchronisation for all."""
+        host = []
+        for t in tensors:
             h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
             h.copy_(t, non_blocking=True)
-            host[k] = h
+            host.append(h)
         torch.cuda.current_stream(self.device).synchronize()
-        return {k: h.numpy() for k, h in host.items()}
+        return [h.numpy() for h in host]
 
     def full_state(self):
         """All particle fields in original order as float32 device tensors:

@@ -45,7 +45,8 @@ class ParticleIO:
         _lib.check(lib.mpm_quantize_particles(st.data_ptr(), st.shape[1], n, ranges.data_ptr(), xv.data_ptr(), s),
                    "mpm_quantize_particles")
         _lib.check(lib.mpm_unpack_colors(solver._color.data_ptr(), n, rgb.data_ptr(), s), "mpm_unpack_colors")
-        return (ranges.cpu().numpy().reshape(2, 3, 2), xv.cpu().numpy().view(np.uint32), rgb.cpu().numpy())
+        ranges_h, xv_h, rgb_h = solver._to_host(ranges, xv, rgb)
+        return ranges_h.reshape(2, 3, 2), xv_h.view(np.uint32), rgb_h
 
     @staticmethod
     def write_particles(solver, fn, slice_size=1000000):

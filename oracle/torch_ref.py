@@ -16,7 +16,6 @@ against its central finite differences).
 """
 from __future__ import annotations
 
-import math
 
 import torch
 

@@ -19,7 +19,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from ._lib import KIND_BOX, KIND_SPHERE, KIND_SURFACE, NROWS, ROW_C, ROW_F, ROW_ID, ROW_JP, ROW_MAT, ROW_V, ROW_X
+from ._lib import KIND_BOX, KIND_SURFACE, NROWS, ROW_C, ROW_F, ROW_ID, ROW_JP, ROW_MAT, ROW_V, ROW_X
 
 MARGIN = 8  # grid nodes kept around each scene's domain
 

@@ -24,7 +24,7 @@ import ctypes
 import torch
 
 from . import _lib
-from ._lib import NROWS, ROW_C, ROW_EP, ROW_F, ROW_ID, ROW_JP, ROW_MAT, ROW_V, ROW_X
+from ._lib import NROWS, ROW_C, ROW_EP, ROW_F, ROW_ID, ROW_V, ROW_X
 from .mpm_solver import MPMSolver
 
 GROWS = 26  # dL/dx 3, dL/dv 3, dL/dC 9, dL/dF 9, dL/dJp 1, dL/dE 1

@@ -32,7 +32,6 @@ def test_slot_layout_host_logic():
 
 @pytest.mark.gpu
 def test_batched_matches_independent_solvers():
-    import torch
     from taichi_elements_gb300.batched import BatchedMPM
     from taichi_elements_gb300.mpm_solver import MPMSolver
     sc = small_scenes()

@@ -8,7 +8,6 @@ Tolerances (GPU float32 vs oracle float64, one substep from one state):
 and never worse than 4x the float32 oracle's own error against float64.
 Trajectories: positions after 100 substeps within rel L2 1e-3 of float64.
 """
-import ctypes
 
 import numpy as np
 import pytest

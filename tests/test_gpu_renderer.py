@@ -3,7 +3,6 @@
 light transport in distribution (the random streams differ)."""
 import numpy as np
 import pytest
-import torch
 
 from oracle import renderer_ref as R
 from taichi_elements_gb300 import scenes

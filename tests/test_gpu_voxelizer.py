@@ -3,7 +3,6 @@ the CPU restatement: voxel counts bit-exact; seeded particles one per
 inside voxel at the default density, each inside its voxel."""
 import numpy as np
 import pytest
-import torch
 
 from oracle import voxelizer_ref as V
 from taichi_elements_gb300 import scenes

@@ -130,6 +130,35 @@ def test_one_substep_parity(scene_fn, n_pre):
         assert g <= max(TOL[k], 4 * f32), f"{k}: gpu {g:.3g} vs f32-oracle {f32:.3g}"
 
 
+def _dense_swirl_scene():
+    """30,000 particles in a cube of ~3.8 cells per side (about 500 per cell)
+    turning at 20 rad/s: cells hold far more than 64 particles, so ranks of
+    64 and above take the arrival path of the binning while particles keep
+    crossing cells."""
+    rng = np.random.default_rng(21)
+    n = 30000
+    c = np.array([0.5, 0.5, 0.5], np.float32)
+    x = (c - 0.06 + 0.12 * rng.random((n, 3))).astype(np.float32)
+    w = np.array([0.0, 20.0, 5.0])
+    v = np.cross(w, x - c).astype(np.float32)
+    mat = np.where(np.arange(n) % 2 == 0, scenes.WATER, scenes.ELASTIC).astype(np.int32)
+    return scenes.Scene("dense_swirl_32", (32, 32, 32), x, v, mat, 20)
+
+
+def test_one_substep_parity_dense_cells():
+    sc = _dense_swirl_scene()
+    keys = np.floor(sc.x.astype(np.float32) * np.float32(32) - np.float32(0.5)).astype(np.int64)
+    _, counts = np.unique(keys, axis=0, return_counts=True)
+    assert counts.max() > 64
+    s = _evolve(sc, 10)
+    s._check_status()
+    errs = _one_substep_errors(s, sc.default_dt)
+    for k, (g, f32) in errs.items():
+        assert g <= max(TOL[k], 4 * f32), f"{k}: gpu {g:.3g} vs f32-oracle {f32:.3g}"
+    s.substep(sc.default_dt)
+    s._check_status()
+
+
 def test_trajectory_100_substeps_four_materials():
     sc = scenes.four_materials_128(per_cube=20000)
     s = sc.make_solver()

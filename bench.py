@@ -678,9 +678,8 @@ def run_adjoint_measure(n_substeps=2000, checkpoint_every=50):
     with respect to initial velocities and E."""
     import torch
 
-    from oracle.torch_ref import com_loss  # loss definition only
     from taichi_elements_gb300 import scenes
-    from taichi_elements_gb300.differentiable import Rollout, rollout_positions
+    from taichi_elements_gb300.differentiable import Rollout, com_loss, rollout_positions
     from taichi_elements_gb300.mpm_solver import MPMSolver
     sc = scenes.elastic_on_water()
     rng = np.random.default_rng(5)

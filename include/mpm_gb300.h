@@ -256,8 +256,12 @@ int mpm_p2g_adj(const MpmParams *p, void *ws, int64_t cap, int64_t n, const floa
  *     fits 16 MiB (about 4,000 blocks of 4^3 nodes, e.g. a 48^3 grid with the
  *     solver's default margins).  Larger inputs return MPM_E_CAPACITY before
  *     any device work.
- *   - The first call on a device looks up the array's device address; make
- *     that first call before any stream capture.
+ *   - The first call on a device looks up the array's device address and
+ *     keeps it for the life of the process; make that first call before any
+ *     stream capture, and do not use the library across a cudaDeviceReset
+ *     (the kept address would then be stale).
+ *   - Single scenes only: batched parameter blocks (n_scenes > 0) and packed
+ *     storage (quant) return MPM_E_INVALID.
  *   - Every call bins all particles itself and clears the scratch it uses,
  *     since the array keeps the previous call's contents; calls that overlap
  *     on the GPU (other streams, other threads) share the array and race.

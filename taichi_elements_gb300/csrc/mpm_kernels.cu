@@ -567,10 +567,13 @@ __global__ __launch_bounds__(256) void k_grid(const MpmParams P, const MpmParams
 
 // ---------------------------------------------------------------- G2P ----
 
-// KEEP: particles that stay in their cell keep their rank there (bin_one
-// with the old key and rank; a particle that leaves marks its old rank in
-// the old cell's leave mask, which k_scatter subtracts from the stayers').
-template <bool BATCH, bool Q, bool KEEP>
+// BIN selects the next substep's binning: kBinKeep - particles that stay in
+// their cell keep their rank there (bin_one with the old key and rank; a
+// particle that leaves marks its old rank in the old cell's leave mask, which
+// k_scatter subtracts from the stayers'); kBinPlain - ranks from arrival
+// order; kBinNone - no binning (the caller bins from scratch next time).
+constexpr int kBinNone = 0, kBinPlain = 1, kBinKeep = 2;
+template <bool BATCH, bool Q, int BIN>
 __global__ __launch_bounds__(kG2PThreads, 8) void k_g2p(const MpmParams P, const MpmParams *tab, const Ws w,
                                                        float *__restrict__ st, int64_t cap, float dt,
                                                        float *maxv_out) {
@@ -662,12 +665,12 @@ __global__ __launch_bounds__(kG2PThreads, 8) void k_g2p(const MpmParams P, const
         ld_v<Q>(st, cap, j, vv);
       }
       vmax = fmaxf(vmax, fmaxf(fabsf(vv[0]), fmaxf(fabsf(vv[1]), fabsf(vv[2]))));
-      if (KEEP) {  // next substep's build_pid, keeping the rank of a stayer
+      if (BIN == kBinKeep) {  // next substep's build_pid, keeping the rank of a stayer
         const int old_key = cell_key(P, b);
         const int r_old = w.slot_rank[j];
         const int key = bin_one<BATCH>(P, tab, w, j, x[0], x[1], x[2], matword, bad, old_key, r_old);
         if (key != old_key && (unsigned)r_old < 64u) atomicOr(&w.leave[old_key], 1ull << r_old);
-      } else {
+      } else if (BIN == kBinPlain) {
         bin_one<BATCH>(P, tab, w, j, x[0], x[1], x[2], matword, bad);  // next substep's build_pid
       }
     }
@@ -959,15 +962,15 @@ static const DevInfo *dev_info() {
     int a = 0, b = 0, c = 0, a2 = 0, b2 = 0, c2 = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_p2g<false, false, false>, kP2GThreads, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_p2g<true, false, false>, kP2GThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_g2p<false, false, true>, kG2PThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_g2p<false, false, kBinKeep>, kG2PThreads, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a2, k_p2g<false, true, false>, kP2GThreads, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_p2g<true, true, false>, kP2GThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c2, k_g2p<true, false, false>, kG2PThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c2, k_g2p<true, false, kBinPlain>, kG2PThreads, 0);
     int f = 0, aq = 0, bq = 0, cq = 0, fq = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, k_g2p2g<false>, kP2GThreads, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&aq, k_p2g<false, false, true>, kP2GThreads, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bq, k_p2g<true, false, true>, kP2GThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cq, k_g2p<false, true, true>, kG2PThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cq, k_g2p<false, true, kBinKeep>, kG2PThreads, 0);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fq, k_g2p2g<true>, kP2GThreads, 0);
     d.g2p2g_ctas = sms * (f > 0 ? f : 1);
     d.p2g_q_ctas = sms * (aq > 0 ? aq : 1);
@@ -1121,10 +1124,10 @@ int mpm_g2p(const MpmParams *p, void *ws, int64_t cap, int64_t n, float *nxt, fl
   Ws w;
   ws_layout(*p, cap, (char *)ws, &w);
   if (p->quant)
-    k_g2p<false, true, true><<<di->g2p_q_ctas, kG2PThreads, 0, (cudaStream_t)stream>>>(*p, nullptr, w, nxt, cap, dt,
+    k_g2p<false, true, kBinKeep><<<di->g2p_q_ctas, kG2PThreads, 0, (cudaStream_t)stream>>>(*p, nullptr, w, nxt, cap, dt,
                                                                                  maxv_out);
   else
-    k_g2p<false, false, true><<<di->g2p_ctas, kG2PThreads, 0, (cudaStream_t)stream>>>(*p, nullptr, w, nxt, cap, dt,
+    k_g2p<false, false, kBinKeep><<<di->g2p_ctas, kG2PThreads, 0, (cudaStream_t)stream>>>(*p, nullptr, w, nxt, cap, dt,
                                                                                 maxv_out);
   return last_error();
 }
@@ -1145,8 +1148,8 @@ int mpm_g2p_bin_into(const MpmParams *p, void *ws, void *ws_bins, int64_t cap, i
   w.cellkey = wb.cellkey;
   w.stay_rank = wb.stay_rank;
   w.arr_cnt = wb.arr_cnt;
-  k_g2p<false, false, false><<<di->g2p_ctas, kG2PThreads, 0, (cudaStream_t)stream>>>(*p, nullptr, w, nxt, cap, dt,
-                                                                                     maxv_out);
+  k_g2p<false, false, kBinPlain><<<di->g2p_ctas, kG2PThreads, 0, (cudaStream_t)stream>>>(*p, nullptr, w, nxt, cap,
+                                                                                         dt, maxv_out);
   return last_error();
 }
 
@@ -1225,13 +1228,13 @@ int mpm_batch_substep(const MpmParams *p, const MpmParams *scenes, void *ws, int
   else
     k_p2g<false, true, false><<<di->p2g_b_ctas, kP2GThreads, 0, s>>>(*p, scenes, w, cur, nxt, cap, 0.0f);
   k_grid<true><<<di->sms * 8, 256, 0, s>>>(*p, scenes, w, 0.0f);
-  k_g2p<true, false, false><<<di->g2p_b_ctas, kG2PThreads, 0, s>>>(*p, scenes, w, nxt, cap, 0.0f, maxv_out);
+  k_g2p<true, false, kBinPlain><<<di->g2p_b_ctas, kG2PThreads, 0, s>>>(*p, scenes, w, nxt, cap, 0.0f, maxv_out);
   return last_error();
 }
 
 int mpm_substep_noalloc(const MpmParams *p, int64_t cap, int64_t n, const float *cur, float *nxt, float dt,
                         float *maxv_out, void *stream) {
-  if (!params_ok(p) || p->quant || !cur || !nxt || n < 0 || n > cap) return MPM_E_INVALID;
+  if (!params_ok(p) || p->quant || p->n_scenes > 0 || !cur || !nxt || n < 0 || n > cap) return MPM_E_INVALID;
   if (n > kStaticMaxParticles) return MPM_E_CAPACITY;
   const size_t bytes = ws_layout(*p, kStaticMaxParticles, nullptr, nullptr);
   if (bytes > kStaticScratchBytes) return MPM_E_CAPACITY;
@@ -1260,7 +1263,8 @@ int mpm_substep_noalloc(const MpmParams *p, int64_t cap, int64_t n, const float 
     else
       k_p2g<false, false, false><<<di->p2g_ctas, kP2GThreads, 0, s>>>(*p, nullptr, w, cur, nxt, cap, dt);
     k_grid<false><<<di->sms * 8, 256, 0, s>>>(*p, nullptr, w, dt);
-    k_g2p<false, false, false><<<di->g2p_ctas, kG2PThreads, 0, s>>>(*p, nullptr, w, nxt, cap, dt, maxv_out);
+    // the next call bins from scratch, so G2P skips the binning
+    k_g2p<false, false, kBinNone><<<di->g2p_ctas, kG2PThreads, 0, s>>>(*p, nullptr, w, nxt, cap, dt, maxv_out);
   }
   return last_error();
 }

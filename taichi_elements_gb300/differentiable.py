@@ -313,3 +313,12 @@ def rollout_positions(rollout: Rollout, v0: torch.Tensor, E: torch.Tensor) -> to
     """Final positions of `rollout` as a differentiable function of the
     initial velocities v0 (n,3) and Young's moduli E (n,)."""
     return _RolloutFunction.apply(v0, E, rollout)
+
+
+def com_loss(x: torch.Tensor, material: torch.Tensor, target: torch.Tensor) -> torch.Tensor:
+    """The differentiable workload's loss: the squared distance of the
+    elastic particles' centre of mass from a target point,
+    |mean(x[material == 1]) - target|^2."""
+    sel = material == MPMSolver.material_elastic
+    com = x[sel].mean(0)
+    return ((com - target)**2).sum()

@@ -77,3 +77,74 @@ def lib_call(solver, name, *args):
     p = solver.params
     rc = getattr(solver._lib, name)(ctypes.byref(p), *args)
     _lib.check(rc, name)
+
+
+def run_phases(solver, dt):
+    """One substep through the C ABI phase by phase; returns the binning
+    views and snapshots of the grid after P2G and after the grid update."""
+    import torch
+    solver._prepare(dt)
+    ws, cap, n = solver._ws.data_ptr(), solver._cap, solver.n_particles
+    cur = solver._state[solver._cur].data_ptr()
+    nxt = solver._state[1 - solver._cur].data_ptr()
+    st = torch.cuda.current_stream().cuda_stream
+    lib_call(solver, "mpm_bin_finalize", ws, cap, n, st)
+    views = solver.views()
+    out = {}
+    lib_call(solver, "mpm_p2g", ws, cap, n, cur, nxt, dt, st)
+    out['mom'] = gpu_grid(views, 'grid_mom')
+    lib_call(solver, "mpm_grid_update", ws, cap, dt, st)
+    out['vel'] = gpu_grid(views, 'grid_vel')
+    lib_call(solver, "mpm_g2p", ws, cap, n, nxt, dt, None, st)
+    solver._cur = 1 - solver._cur
+    torch.cuda.synchronize()
+    return views, out
+
+
+# ------------------------------------------- reference-run fixtures ----
+
+REF_CASES = ["mixed_24", "walls_24", "unbounded_24", "no_plasticity_24"]
+
+
+def ref_fixture(name):
+    """tests/golden/ref_<name>.npz: outputs of the reference's own kernels
+    (tests/golden/make_reference_golden.py) as a dict of numpy arrays."""
+    import os
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", f"ref_{name}.npz")
+    with np.load(path) as g:
+        return {k: g[k] for k in g.files}
+
+
+def ref_postprocess(g):
+    """The fixture's collider list in the oracle's record form, after the
+    bounding box the reference's constructor adds first."""
+    import ast
+    pp = [dict(kind=O.KIND_BOX, surface=0)]
+    for c in ast.literal_eval(str(g["postprocess"])):
+        if c["kind"] == "surface":
+            pp.append(dict(kind=O.KIND_SURFACE, surface=c["surface"], point=c["point"], normal=c["normal"],
+                           friction=c["friction"]))
+        else:
+            pp.append(dict(kind=O.KIND_SPHERE, surface=c["surface"], point=c["center"], radius=c["radius"]))
+    return pp
+
+
+def ref_kw(g):
+    import ast
+    return ast.literal_eval(str(g["kw"])) if "kw" in g else {}
+
+
+def ref_config(g):
+    kw = ref_kw(g)
+    return O.Config(res=tuple(int(r) for r in g["res"]), postprocess=ref_postprocess(g),
+                    unbounded=kw.get("unbounded", False), water_density=kw.get("water_density", 1.0),
+                    support_plasticity=kw.get("support_plasticity", True))
+
+
+def ref_particles(g, dtype=np.float64):
+    n = int(g["n"])
+    Jp = g["in_Jp"] if "in_Jp" in g else np.ones(n)
+    C = g["in_C"] if "in_C" in g else np.zeros((n, 3, 3))
+    return O.Particles(np.ascontiguousarray(g["in_x"], dtype), np.ascontiguousarray(g["in_v"], dtype),
+                       np.ascontiguousarray(C, dtype), np.ascontiguousarray(g["in_F"], dtype),
+                       np.ascontiguousarray(Jp, dtype), np.ascontiguousarray(g["in_material"], np.int32))

@@ -18,7 +18,8 @@ import pytest
 import torch
 
 from oracle import oracle as O
-from oracle.torch_ref import TorchMPM, com_loss
+from oracle.torch_ref import TorchMPM
+from oracle.torch_ref import com_loss as com_loss_ref
 from taichi_elements_gb300 import scenes
 
 pytestmark = pytest.mark.gpu
@@ -38,7 +39,7 @@ def make_case(seed=3, n_each=2000):
 
 
 def gpu_grads(sc, v0, E, nsub=NSUB, k=K, keep_workspaces=None):
-    from taichi_elements_gb300.differentiable import Rollout, rollout_positions
+    from taichi_elements_gb300.differentiable import Rollout, com_loss, rollout_positions
     from taichi_elements_gb300.mpm_solver import MPMSolver
     s = MPMSolver(sc.res, per_particle_E=True)
     for m in (0, 1):
@@ -64,7 +65,7 @@ def torch_grads(sc, v0, E):
     e = torch.tensor(E, dtype=torch.float64, requires_grad=True)
     mat = torch.tensor(sc.material)
     xT = T.rollout(x0, v, mat, e, sc.default_dt, NSUB)
-    L = com_loss(xT, mat, torch.tensor(sc.target))
+    L = com_loss_ref(xT, mat, torch.tensor(sc.target))
     L.backward()
     return float(L), xT.detach().numpy(), v.grad.numpy(), e.grad.numpy()
 

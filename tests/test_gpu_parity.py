@@ -13,33 +13,13 @@ import numpy as np
 import pytest
 import torch
 
-from helpers import gpu_grid, lib_call, oracle_config, particles_from_solver, rel_inf, block_coords, window_lookup
+from helpers import (block_coords, lib_call, oracle_config, particles_from_solver, rel_inf, run_phases,
+                     window_lookup)
 from oracle import oracle as O
 from taichi_elements_gb300 import scenes
 from taichi_elements_gb300.mpm_solver import MPMSolver, MPMError
 
 pytestmark = pytest.mark.gpu
-
-
-def run_phases(solver, dt):
-    """One substep through the C ABI phase by phase; returns the binning
-    views and snapshots of the grid after P2G and after the grid update."""
-    solver._prepare(dt)
-    ws, cap, n = solver._ws.data_ptr(), solver._cap, solver.n_particles
-    cur = solver._state[solver._cur].data_ptr()
-    nxt = solver._state[1 - solver._cur].data_ptr()
-    st = torch.cuda.current_stream().cuda_stream
-    lib_call(solver, "mpm_bin_finalize", ws, cap, n, st)
-    views = solver.views()
-    out = {}
-    lib_call(solver, "mpm_p2g", ws, cap, n, cur, nxt, dt, st)
-    out['mom'] = gpu_grid(views, 'grid_mom')
-    lib_call(solver, "mpm_grid_update", ws, cap, dt, st)
-    out['vel'] = gpu_grid(views, 'grid_vel')
-    lib_call(solver, "mpm_g2p", ws, cap, n, nxt, dt, None, st)
-    solver._cur = 1 - solver._cur
-    torch.cuda.synchronize()
-    return views, out
 
 
 def test_binning_bit_exact_water_cube():

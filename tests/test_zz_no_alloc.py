@@ -31,9 +31,24 @@ def _gather(solver, buf, row0, ncols):
     return out.cpu().numpy()
 
 
-def test_noalloc_substep_matches_regular_substep():
+def _solver(per_particle_E):
     sc = scenes.smoke_scene()
-    s = sc.make_solver()
+    if not per_particle_E:
+        return sc, sc.make_solver()
+    # per-particle Young's modulus, spread over a factor of e around the
+    # solver's E, so the has_Ep branch of P2G is the one that runs
+    s = sc.make_solver(per_particle_E=True)
+    rng = np.random.default_rng(11)
+    E = (s.E * np.exp(rng.uniform(-0.5, 0.5, s.n_particles))).astype(np.float32)
+    st = s._state[s._cur]
+    ids = st[_lib.ROW_ID, :s.n_particles].view(torch.int32).long()
+    st[_lib.ROW_EP, :s.n_particles] = torch.as_tensor(E, device=s.device)[ids]
+    return sc, s
+
+
+@pytest.mark.parametrize("per_particle_E", [False, True])
+def test_noalloc_substep_matches_regular_substep(per_particle_E):
+    sc, s = _solver(per_particle_E)
     dt = sc.default_dt
     s._prepare(dt)  # regular path: workspace allocated, particles binned
     lib = s._lib

@@ -22,7 +22,10 @@
  *   24 Jp, 25 material (int32 bits), 26 original particle id (int32 bits),
  *   27 per-particle Young's modulus (used only when MpmParams.has_Ep != 0).
  * The engine ping-pongs between two such buffers: a substep reads buffer
- * `cur` in any order and writes buffer `nxt` sorted by grid block.
+ * `cur` in any order and writes buffer `nxt` sorted by grid block.  `cap`
+ * must be a multiple of 32 and the buffers 16-byte aligned: P2G stages
+ * 128-byte segments of the rows with bulk copies (entry points that run P2G
+ * return MPM_E_INVALID otherwise).
  *
  * With MpmParams.quant != 0 (MPMSolver(quant=True), engine/mpm_solver.py
  * :106-127 and :216-262) the buffers hold MPM_QROWS rows of 32-bit words:
@@ -53,6 +56,7 @@ extern "C" {
 #define MPM_STATUS_NONFINITE 2u    /* NaN/Inf particle position */
 #define MPM_STATUS_TABLE_OVERFLOW 4u
 #define MPM_STATUS_UNSUPPORTED 8u     /* adjoint met a material it does not differentiate */
+#define MPM_STATUS_TIMEOUT 16u        /* a bounded wait for staged data gave up (results invalid) */
 
 /* error codes */
 #define MPM_OK 0

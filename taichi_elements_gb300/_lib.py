@@ -21,6 +21,7 @@ STATUS_OUT_OF_GRID = 1
 STATUS_NONFINITE = 2
 STATUS_TABLE_OVERFLOW = 4
 STATUS_UNSUPPORTED = 8
+STATUS_TIMEOUT = 16
 
 # Row indices of the particle-state buffer.
 ROW_X, ROW_V, ROW_C, ROW_F, ROW_JP, ROW_MAT, ROW_ID, ROW_EP = 0, 3, 6, 15, 24, 25, 26, 27

@@ -32,11 +32,13 @@ struct Ws {
   int32_t *gblocks;   // [nblk] compact grid-active blocks (ascending)
   int32_t *flag_tiles;  // [2 * nflagtiles]
   int32_t *pb_count, *pb_start, *pb_lvl, *pb_item;  // [nblk] each
+  int32_t *pb_nlev;   // [nblk] levels (largest cell count) of each particle block
   int32_t *pb_tiles;  // [3 * nstattiles]
   unsigned long long *lvl_mask;  // [cap]
   int32_t *lvl_L;                // [cap]
   int2 *items;                   // [cap/32 + nblk + 1]
   int32_t *cellkey, *pid;  // [cap]
+  int32_t *inv;            // [cap] sorted slot of the particle at input slot i (pid's inverse)
   int32_t *slot_rank;  // [cap] rank inside its cell of the particle at sorted slot j
   int32_t *stay_rank;  // [cap] next rank of a particle that stays in its cell, else -1
   int32_t *cell_cnt;              // [nblk * 64]
@@ -75,12 +77,14 @@ inline size_t ws_layout(const MpmParams &p, int64_t cap, char *base, Ws *w) {
   t.pb_start = (int32_t *)take(nblk * 4);
   t.pb_lvl = (int32_t *)take(nblk * 4);
   t.pb_item = (int32_t *)take(nblk * 4);
+  t.pb_nlev = (int32_t *)take(nblk * 4);
   t.pb_tiles = (int32_t *)take((size_t)3 * nst * 4);
   t.lvl_mask = (unsigned long long *)take((size_t)cap * 8);
   t.lvl_L = (int32_t *)take((size_t)cap * 4);
   t.items = (int2 *)take((size_t)items_cap * 8);
   t.cellkey = (int32_t *)take((size_t)cap * 4);
   t.pid = (int32_t *)take((size_t)cap * 4);
+  t.inv = (int32_t *)take((size_t)cap * 4);
   t.slot_rank = (int32_t *)take((size_t)cap * 4);
   t.stay_rank = (int32_t *)take((size_t)cap * 4);
   t.cell_cnt = (int32_t *)take((size_t)nblk * kBlockCells * 4);

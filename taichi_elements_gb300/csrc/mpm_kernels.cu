@@ -33,13 +33,16 @@
 #include <mutex>
 
 #include "mpm_common.cuh"
+#include "tma.cuh"
 
 namespace mpm {
 
-constexpr int kP2GThreads = 128;
-// P2G CTAs per SM the register budget is sized for (128 threads each)
-#ifndef MPM_P2G_MIN_CTAS
-#define MPM_P2G_MIN_CTAS 4
+// fused G2P2G: CTAs of 128 threads, per-warp tiles; CTAs per SM the
+// register budget is sized for
+constexpr int kFusedThreads = 128;
+constexpr int kFusedWarps = kFusedThreads / 32;
+#ifndef MPM_FUSED_MIN_CTAS
+#define MPM_FUSED_MIN_CTAS 4
 #endif
 constexpr int kG2PThreads = 128;
 
@@ -319,6 +322,7 @@ __global__ __launch_bounds__(256) void k_pb_levels(const MpmParams P, const Ws w
       if (lane == 0) set_status(w, MPM_STATUS_TABLE_OVERFLOW);
       mx = 0;
     }
+    if (lane == 0) w.pb_nlev[k] = mx;
     int L = 0;
     for (int r = 0; r < mx; ++r) {
       const unsigned m0 = __ballot_sync(0xffffffffu, c0 > r);
@@ -344,6 +348,7 @@ __global__ __launch_bounds__(256) void k_pb_levels(const MpmParams P, const Ws w
 __global__ void k_scatter(const MpmParams P, const Ws w, int64_t n) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  w.inv[i] = -1;  // until the particle's sorted slot is known
   const int key = w.cellkey[i];
   // Rank inside the cell: particles that stayed in their cell keep their
   // order (ranks 0 .. N - A - 1, set in G2P); the A others take the ranks
@@ -370,6 +375,7 @@ __global__ void k_scatter(const MpmParams P, const Ws w, int64_t n) {
     return;
   }
   w.pid[pos] = (int)i;
+  w.inv[i] = pos;
   w.slot_rank[pos] = r;
 }
 
@@ -394,152 +400,310 @@ __global__ __launch_bounds__(256) void k_cell_clear(const MpmParams P, const Ws 
 
 // ---------------------------------------------------------------- P2G ----
 //
-// Each warp scatters into its own float4 tile (m, mv) of the block's 6^3
-// nodes with plain shared-memory read-modify-writes, one stencil offset at a
-// time with a __syncwarp() between offsets.  Within one offset step the lanes
-// touch distinct nodes as long as their cells differ, which the rank-major
-// particle order guarantees inside a level; the rare lanes that share a cell
-// (a warp straddling two short levels) are found with __match_any_sync and
-// scatter in later rounds.  No shared-memory float atomics are used.  At the
-// end of a work item the warps' tiles are summed and flushed to the grid with
-// one float4 global reduction per touched node.
+// P2G visits the particles in the order of the state buffer `cur` (the
+// sorted order of the previous substep), 32 consecutive slots per warp step,
+// so each state row of a step is one contiguous 128-byte segment.  Each warp
+// runs its own two-stage pipeline: one lane issues bulk copies (TMA) of the
+// next step's rows and of their sorted slots (`inv`) into one of two shared
+// buffers while the warp works on the current step, so the row loads never
+// stall the warp.  Per particle: constitutive update (engine/mpm_solver.py
+// :506-574), the updated state written to its sorted slot `inv[i]` of `nxt`,
+// and the APIC scatter (:576-584) into the warp's 8^3 float4 tile of grid
+// nodes with plain shared-memory read-modify-writes.  The tile is anchored at
+// the step's smallest base cell: the particles of a step are the 32 cells of
+// one level of one block of the previous binning, so their base cells lie in
+// a 6-wide range and several steps share one anchor.  When a step does not fit
+// the tile is flushed to the grid (one float4 reduction per touched node) and
+// re-anchored; the rare particle outside a fresh anchor scatters with global
+// atomics.  Lanes of a step hold distinct cells (rank-major order), so the 27
+// node updates of a pass never collide; particles that moved into a shared
+// cell are found with __match_any_sync and scatter in later passes.  Steps
+// are taken from a queue in guided runs of consecutive steps.
 
-constexpr int kP2GWarps = kP2GThreads / 32;
+constexpr int kP2GWarps = 4;
+// P2G CTAs per SM the register budget is sized for (168 registers at 3; 4 would
+// fit the shared memory but spill)
+#ifndef MPM_P2G_MIN_CTAS
+#define MPM_P2G_MIN_CTAS 3
+#endif
+constexpr int kP2GThreads = kP2GWarps * 32;
+constexpr int kP2GRun = 16;                    // longest run of steps per queue grab
+constexpr int kP2GQueue = 5, kP2GDone = 6;     // counters[]: run queue, warps done
+constexpr int kP2GTileW = 8;                   // tile nodes per axis
+// tile index = tx * 76 + ty * 9 + tz: the x stride is 4 mod 8, so the 8 lanes
+// of a quarter-warp (cells z = 0..3 at x = 2k, 2k+1) hit 8 bank groups
+constexpr int kP2GTileSX = 76, kP2GTileSY = 9;
+constexpr int kP2GTileN = 7 * kP2GTileSX + 7 * kP2GTileSY + 8;  // 603
+constexpr int kP2GRowsMax = MPM_NROWS + 1;     // state rows + inv
 
-__device__ __forceinline__ float4 f4add(float4 a, float4 b) {
-  return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+// Per-warp shared memory.  A tiled tensor copy needs a 128-byte-aligned
+// shared destination: the struct (buffers first) is 128-byte aligned and its
+// size a multiple of 128, and the dynamic shared base is 128-byte aligned.
+struct __align__(128) P2GWarpSmem {
+  float buf[kP2GRowsMax][32];
+  float4 tile[kP2GTileN + 1];
+  unsigned long long bar;
+};
+static_assert(sizeof(P2GWarpSmem) % 128 == 0, "per-warp staging buffers must stay 128-byte aligned");
+constexpr size_t kP2GSmem = sizeof(P2GWarpSmem) * kP2GWarps;
+
+template <bool Q, bool HAS_EP>
+struct P2GRows {  // rows staged per step (the state rows P2G reads)
+  static constexpr int N = Q ? MPM_QROWS : (HAS_EP ? MPM_NROWS : MPM_NROWS - 1);
+};
+
+__device__ __forceinline__ int p2g_tile_index(int tx, int ty, int tz) {
+  return tx * kP2GTileSX + ty * kP2GTileSY + tz;
+}
+
+// Flushes the warp's tile anchored at node o (window-relative) to the grid
+// and clears it.
+__device__ __forceinline__ void p2g_tile_flush(const MpmParams &P, const Ws &w, float4 *tile, const int (&o)[3],
+                                               int lane) {
+  for (int t = lane; t < kP2GTileW * kP2GTileW * kP2GTileW; t += 32) {
+    const int tx = t >> 6, ty = (t >> 3) & 7, tz = t & 7;
+    float4 &nd = tile[p2g_tile_index(tx, ty, tz)];
+    const float4 g = nd;
+    if (g.x != 0.0f) {
+      const int gx = o[0] + tx, gy = o[1] + ty, gz = o[2] + tz;
+      if (gx < P.win_nb[0] * 4 && gy < P.win_nb[1] * 4 && gz < P.win_nb[2] * 4)
+        atomicAdd(&w.grid_mom[node_addr(P, gx, gy, gz)], g);
+      nd = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+  }
+  __syncwarp();
+}
+
+// The next step of this warp (warp-uniform; -1 when the queue is empty).
+// Lane 0 keeps the cursor (q_next, q_end) of its current run.  Runs are
+// guided: a grab takes about a (2 * warps)-th of the steps left, at most
+// kP2GRun, so the last grabs are single steps and warps finish together.
+__device__ __forceinline__ int p2g_next_step(const Ws &w, int lane, int nsteps, int nwarps, int &q_next,
+                                             int &q_end) {
+  int g = -1;
+  if (lane == 0) {
+    if (q_next >= q_end) {
+      const int seen = *(volatile const int *)&w.counters[kP2GQueue];
+      const int len = max(1, min(kP2GRun, (nsteps - seen) / (2 * nwarps)));
+      const int r = atomicAdd(&w.counters[kP2GQueue], len);
+      q_next = min(r, nsteps);
+      q_end = min(r + len, nsteps);
+    }
+    if (q_next < q_end) g = q_next++;
+  }
+  return __shfl_sync(0xffffffffu, g, 0);
+}
+
+// Stages step g: one tensor-map box of NR rows x 32 slots and the 32 sorted
+// slots, completing on the warp's mbarrier.
+template <int NR>
+__device__ __forceinline__ void p2g_issue(P2GWarpSmem &sm, const CUtensorMap &rows_map, const Ws &w, int g,
+                                          int lane) {
+  if (lane == 0) {
+    fence_proxy_async_smem();
+    mbar_arrive_expect_tx(&sm.bar, (NR + 1) * 128);
+    tma_load_2d(sm.buf[0], &rows_map, g * 32, 0, &sm.bar);
+    bulk_g2s(sm.buf[NR], w.inv + (int64_t)g * 32, 128, &sm.bar);
+  }
 }
 
 template <bool HAS_EP, bool BATCH, bool Q>
 __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_p2g(const MpmParams P, const MpmParams *tab, const Ws w,
-                                                       const float *__restrict__ cur,
-                                                       float *__restrict__ nxt, int64_t cap, float dt) {
-  // two tiles per warp: a lane whose cell already appears in an earlier lane
-  // of the same group (the second particle of a cell when a group straddles
-  // two short levels) scatters into the second tile in the same pass
-  __shared__ float4 tiles[kP2GWarps][2][kTileN];
+                                                        const __grid_constant__ CUtensorMap rows_map,
+                                                        const float *__restrict__ cur, float *__restrict__ nxt,
+                                                        int64_t cap, int64_t n, float dt) {
+  using R = PRows<Q>;
+  constexpr int NR = P2GRows<Q, HAS_EP>::N;
+  extern __shared__ __align__(128) unsigned char p2g_smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nitems = (int)min((int64_t)w.counters[2], w.items_cap);
+  P2GWarpSmem &sm = reinterpret_cast<P2GWarpSmem *>(p2g_smem)[warp];
+  const int nsteps = (int)((n + 31) / 32);
+  const int nwarps = (int)gridDim.x * kP2GWarps;
   uint32_t bad = 0;
-  for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
-    const int2 item = w.items[it];
-    const int k = item.x, start = item.y;
-    const int end = (int)min((int64_t)min(start + P.chunk, w.pb_start[k] + w.pb_count[k]), cap);
-    int bx, by, bz;
-    block_coords(P, w.pblocks[k], bx, by, bz);
-    for (int t = lane; t < 2 * kTileN; t += 32) (&tiles[warp][0][0])[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+
+  for (int t = lane; t < kP2GTileN + 1; t += 32) sm.tile[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (lane == 0) {
+    mbar_init(&sm.bar, 1);
+    fence_mbar_init();
+  }
+  __syncwarp();
+
+  // One staging buffer: a step's rows go to registers first, then the next
+  // step's copy is issued into the buffer and lands while this step computes.
+  int q_next = 0, q_end = 0;  // lane 0's cursor in the run queue
+  uint32_t parity = 0u;
+  int g0 = p2g_next_step(w, lane, nsteps, nwarps, q_next, q_end);
+  if (g0 >= 0) p2g_issue<NR>(sm, rows_map, w, g0, lane);
+  bool anchored = false;
+  int o[3] = {0, 0, 0};
+
+  while (g0 >= 0) {
+    if (!mbar_wait(&sm.bar, parity)) {  // the staged rows never arrived: report and leave
+      bad |= MPM_STATUS_TIMEOUT;
+      anchored = false;
+      break;
+    }
+    parity ^= 1u;
+    const float *sb = &sm.buf[0][0];
+    const int64_t i = (int64_t)g0 * 32 + lane;
+    bool act = i < n;
+    // this lane's particle, from the staged rows
+    float x[3], v[3], C[3][3], F[3][3];
+    ld_x<Q>(sb, 32, lane, x);
+    ld_v<Q>(sb, 32, lane, v);
+    ld_F<Q>(sb, 32, lane, F);
+#pragma unroll
+    for (int a = 0; a < 9; ++a) C[a / 3][a % 3] = sb[(R::C + a) * 32 + lane];
+    float Jp = sb[R::Jp * 32 + lane];
+    const int matword = ld_mat<Q>(sb, 32, lane);
+    const float idf = sb[R::Id * 32 + lane];
+    const float Ep = HAS_EP ? sb[R::Ep * 32 + lane] : 0.0f;
+    float xw[2] = {sb[lane], sb[32 + lane]};  // position words (rows 0, 1 and, unpacked, 2)
+    const float x2w = Q ? 0.0f : sb[2 * 32 + lane];
+    float vw[3];  // velocity words, copied unchanged for stationary particles
+#pragma unroll
+    for (int r = 0; r < 3; ++r) vw[r] = (Q && r == 2) ? 0.0f : sb[(R::V + r) * 32 + lane];
+    const int64_t j = __float_as_int(sb[NR * 32 + lane]);
     __syncwarp();
-    for (int j0 = start + warp * 32; j0 < end; j0 += kP2GThreads) {
-      const int j = j0 + lane;
-      bool active = j < end;
-      int64_t i = active ? w.pid[j] : 0;
-      if (active && (i < 0 || i >= cap)) {
-        bad |= MPM_STATUS_TABLE_OVERFLOW;
-        active = false;
+    // the buffer is free: stage the next step into it
+    const int g1 = p2g_next_step(w, lane, nsteps, nwarps, q_next, q_end);
+    if (g1 >= 0) p2g_issue<NR>(sm, rows_map, w, g1, lane);
+
+    if (act && (j < 0 || j >= n)) {
+      bad |= MPM_STATUS_TABLE_OVERFLOW;
+      act = false;
+    }
+    const int mat = matword & 0xFF;
+    if (act) {
+      // carried fields go to the sorted slot right away: the position words,
+      // id and E unchanged, and a stationary particle's velocity (:722)
+      nxt[j] = xw[0];
+      nxt[cap + j] = xw[1];
+      if (!Q) nxt[2 * cap + j] = x2w;
+      nxt[R::Id * cap + j] = idf;
+      if (HAS_EP) nxt[R::Ep * cap + j] = Ep;
+      if (mat == 4) {
+#pragma unroll
+        for (int r = 0; r < (Q ? 2 : 3); ++r) nxt[(R::V + r) * cap + j] = vw[r];
       }
-      int cell = -1 - lane;  // unique per inactive lane
-      // inactive lanes keep zero weights: they read tile nodes but never store
-      float mass = 0.f, q[3] = {0.f, 0.f, 0.f}, adx[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
-      float wt[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
-      int lx = 0, ly = 0, lz = 0;
-      if (active) {
-        using R = PRows<Q>;
-        float x[3], v[3], C[3][3], F[3][3];
-        ld_x<Q>(cur, cap, i, x);
-        const int matword = ld_mat<Q>(cur, cap, i);
-        const int mat = matword & 0xFF;
-        const MpmParams &S = scene_of_particle<BATCH>(P, tab, matword);
-        const float Ep = HAS_EP ? cur[R::Ep * cap + i] : 0.0f;
-        // carried fields go to the sorted position j right away
-        cp_x<Q>(cur, i, nxt, j, cap);
-        nxt[R::Id * cap + j] = cur[R::Id * cap + i];
-        if (HAS_EP) nxt[R::Ep * cap + j] = Ep;
-        const Base b = particle_base(S, x[0], x[1], x[2], bad);
-        ld_v<Q>(cur, cap, i, v);
-        ld_F<Q>(cur, cap, i, F);
+    }
+    const MpmParams &S = scene_of_particle<BATCH>(P, tab, matword);
+    uint32_t bad_base = 0;
+    Base bs = particle_base(S, x[0], x[1], x[2], bad_base);
+    if (act) bad |= bad_base;
+    float mass = 0.f, q[3] = {0.f, 0.f, 0.f}, adx[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+    float wt[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+    if (act) {
+      const P2GOut out = constitutive(S, BATCH ? S.dt : dt, mat, Ep, F, Jp, C);
+      st_F_mat<Q>(nxt, cap, j, F, matword);
+      nxt[R::Jp * cap + j] = Jp;
+      if (mat == 4) {  // stationary: G2P keeps v and C (:722)
 #pragma unroll
-        for (int a = 0; a < 9; ++a) C[a / 3][a % 3] = cur[(R::C + a) * cap + i];
-        float Jp = cur[R::Jp * cap + i];
-        const P2GOut o = constitutive(S, BATCH ? S.dt : dt, mat, Ep, F, Jp, C);
-        st_F_mat<Q>(nxt, cap, j, F, matword);
-        nxt[R::Jp * cap + j] = Jp;
-        if (mat == 4) {  // stationary: G2P keeps v and C (:722)
-#pragma unroll
-          for (int r = 0; r < (Q ? 2 : 3); ++r) nxt[(R::V + r) * cap + j] = cur[(R::V + r) * cap + i];
-#pragma unroll
-          for (int a = 0; a < 9; ++a) nxt[(R::C + a) * cap + j] = C[a / 3][a % 3];
-        }
-        lx = b.b[0] - bx * 4;
-        ly = b.b[1] - by * 4;
-        lz = b.b[2] - bz * 4;
-        if ((unsigned)lx > 3u || (unsigned)ly > 3u || (unsigned)lz > 3u) {  // moved since binning
-          bad |= MPM_STATUS_TABLE_OVERFLOW;
-          active = false;
-          lx = ly = lz = 0;
-        } else {
-          cell = local_cell(lx, ly, lz);
-          bspline_weights(b.fx, wt);
-          mass = o.mass;
-          // APIC scatter, :576-584: node value = w * (m v + A (off - fx) dx)
-#pragma unroll
-          for (int d = 0; d < 3; ++d)
-            q[d] = o.mass * v[d] -
-                   S.dx * (o.affine[d][0] * b.fx[0] + o.affine[d][1] * b.fx[1] + o.affine[d][2] * b.fx[2]);
-#pragma unroll
-          for (int r = 0; r < 3; ++r)
-#pragma unroll
-            for (int c = 0; c < 3; ++c) adx[r][c] = o.affine[r][c] * S.dx;
-        }
+        for (int a = 0; a < 9; ++a) nxt[(R::C + a) * cap + j] = C[a / 3][a % 3];
       }
-      // The k-th lane (k = 0, 1, ...) of a group sharing a cell scatters into
-      // tile k % 2 in pass k / 2; inside one pass and tile all cells differ.
-      const unsigned peers = __match_any_sync(0xffffffffu, cell);
-      const int round_of_lane = __popc(peers & ((1u << lane) - 1u));
-      float4 *tile = tiles[warp][round_of_lane & 1];
-      for (int round = 0;; ++round) {
-        const bool mine = active && (round_of_lane >> 1) == round;
-        const int base_node = (lx * kTileW + ly) * kTileW + lz;
+      bspline_weights(bs.fx, wt);
+      mass = out.mass;
+      // APIC scatter, :576-584: node value = w * (m v + A (off - fx) dx)
 #pragma unroll
-        for (int a = 0; a < 3; ++a)
+      for (int d = 0; d < 3; ++d)
+        q[d] = out.mass * v[d] -
+               S.dx * (out.affine[d][0] * bs.fx[0] + out.affine[d][1] * bs.fx[1] + out.affine[d][2] * bs.fx[2]);
 #pragma unroll
-          for (int bb = 0; bb < 3; ++bb) {
-            const float wab = wt[a][0] * wt[bb][1];
-            float pab[3];
+      for (int r = 0; r < 3; ++r)
 #pragma unroll
-            for (int d = 0; d < 3; ++d) pab[d] = q[d] + adx[d][0] * (float)a + adx[d][1] * (float)bb;
+        for (int c = 0; c < 3; ++c) adx[r][c] = out.affine[r][c] * S.dx;
+    }
+    // anchor the tile: all base cells within [o, o + 5]
+    int lo[3], hi[3];
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-              // unconditional read and arithmetic, predicated store only
-              const float wgt = wab * wt[c][2];
-              float4 *nd = tile + base_node + (a * kTileW + bb) * kTileW + c;
-              float4 g = *nd;
-              g.x = fmaf(wgt, mass, g.x);
-              g.y = fmaf(wgt, fmaf(adx[0][2], (float)c, pab[0]), g.y);
-              g.z = fmaf(wgt, fmaf(adx[1][2], (float)c, pab[1]), g.z);
-              g.w = fmaf(wgt, fmaf(adx[2][2], (float)c, pab[2]), g.w);
-              if (mine) *nd = g;
-              __syncwarp();
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = __reduce_min_sync(0xffffffffu, act ? bs.b[d] : INT32_MAX);
+      hi[d] = __reduce_max_sync(0xffffffffu, act ? bs.b[d] : INT32_MIN);
+    }
+    const bool any = __any_sync(0xffffffffu, act);
+    if (any) {
+      const bool fits = anchored && lo[0] >= o[0] && lo[1] >= o[1] && lo[2] >= o[2] &&
+                        hi[0] <= o[0] + kP2GTileW - 3 && hi[1] <= o[1] + kP2GTileW - 3 &&
+                        hi[2] <= o[2] + kP2GTileW - 3;
+      if (!fits) {
+        if (anchored) p2g_tile_flush(P, w, sm.tile, o, lane);
+        // one cell of slack below: the steps of one block of the previous
+        // binning have base cells in [B - 1, B + 4] (B the block's first
+        // cell), and the first step's smallest is usually B
+#pragma unroll
+        for (int d = 0; d < 3; ++d) o[d] = hi[d] - lo[d] <= kP2GTileW - 4 ? max(lo[d] - 1, 0) : lo[d];
+        anchored = true;
+      }
+    }
+    const int tx0 = bs.b[0] - o[0], ty0 = bs.b[1] - o[1], tz0 = bs.b[2] - o[2];
+    const bool inwin = act && (unsigned)tx0 <= kP2GTileW - 3 && (unsigned)ty0 <= kP2GTileW - 3 &&
+                       (unsigned)tz0 <= kP2GTileW - 3;
+    if (act && !inwin) {  // rare: straight to the grid
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int bb = 0; bb < 3; ++bb)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const int gx = bs.b[0] + a, gy = bs.b[1] + bb, gz = bs.b[2] + c;
+            if (gx >= P.win_nb[0] * 4 || gy >= P.win_nb[1] * 4 || gz >= P.win_nb[2] * 4) continue;
+            const float wgt = wt[a][0] * wt[bb][1] * wt[c][2];
+            float4 g;
+            g.x = wgt * mass;
+            g.y = wgt * (q[0] + adx[0][0] * (float)a + adx[0][1] * (float)bb + adx[0][2] * (float)c);
+            g.z = wgt * (q[1] + adx[1][0] * (float)a + adx[1][1] * (float)bb + adx[1][2] * (float)c);
+            g.w = wgt * (q[2] + adx[2][0] * (float)a + adx[2][1] * (float)bb + adx[2][2] * (float)c);
+            atomicAdd(&w.grid_mom[node_addr(P, gx, gy, gz)], g);
+          }
+    }
+    // tile scatter: one pass per set of lanes with distinct base cells
+    const int cell = inwin ? p2g_tile_index(tx0, ty0, tz0) : -1 - lane;
+    const unsigned peers = __match_any_sync(0xffffffffu, cell);
+    const int round_of_lane = __popc(peers & ((1u << lane) - 1u));
+    const int base_node = inwin ? cell : 0;
+    for (int round = 0;; ++round) {
+      const bool mine = inwin && round_of_lane == round;
+#pragma unroll
+      for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int bb = 0; bb < 3; ++bb) {
+          const float wab = wt[a][0] * wt[bb][1];
+          const float2 p0 = make_float2(mass, fmaf(adx[0][1], (float)bb, fmaf(adx[0][0], (float)a, q[0])));
+          const float2 p1 = make_float2(fmaf(adx[1][1], (float)bb, fmaf(adx[1][0], (float)a, q[1])),
+                                        fmaf(adx[2][1], (float)bb, fmaf(adx[2][0], (float)a, q[2])));
+          const float2 dz0 = make_float2(0.0f, adx[0][2]), dz1 = make_float2(adx[1][2], adx[2][2]);
+          float2 t0 = p0, t1 = p1;
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            // unconditional read and arithmetic, predicated store only
+            const float wgt = wab * wt[c][2];
+            const float2 w2 = make_float2(wgt, wgt);
+            float4 *nd = sm.tile + base_node + a * kP2GTileSX + bb * kP2GTileSY + c;
+            float4 g = *nd;
+            const float2 g01 = __ffma2_rn(w2, t0, make_float2(g.x, g.y));
+            const float2 g23 = __ffma2_rn(w2, t1, make_float2(g.z, g.w));
+            if (mine) *nd = make_float4(g01.x, g01.y, g23.x, g23.y);
+            __syncwarp();
+            if (c < 2) {
+              t0 = __fadd2_rn(t0, dz0);
+              t1 = __fadd2_rn(t1, dz1);
             }
           }
-        if (!__any_sync(0xffffffffu, active && (round_of_lane >> 1) > round)) break;
-      }
+        }
+      if (!__any_sync(0xffffffffu, inwin && round_of_lane > round)) break;
     }
-    __syncthreads();
-    for (int t = threadIdx.x; t < kTileN; t += blockDim.x) {
-      float4 g = tiles[0][0][t];
-      g = f4add(g, tiles[0][1][t]);
-#pragma unroll
-      for (int q = 1; q < kP2GWarps; ++q) g = f4add(f4add(g, tiles[q][0][t]), tiles[q][1][t]);
-      if (g.x != 0.0f) {
-        const int tx = t / 36, ty = (t / 6) % 6, tz = t % 6;
-        const int gx = bx * 4 + tx, gy = by * 4 + ty, gz = bz * 4 + tz;
-        if (gx < P.win_nb[0] * 4 && gy < P.win_nb[1] * 4 && gz < P.win_nb[2] * 4)
-          atomicAdd(&w.grid_mom[node_addr(P, gx, gy, gz)], g);
-      }
-    }
-    __syncthreads();
+    g0 = g1;
   }
+  if (anchored) p2g_tile_flush(P, w, sm.tile, o, lane);
   set_status(w, bad);
+  // the last warp to finish resets the queue, so the kernel can run again
+  if (lane == 0) {
+    __threadfence();
+    if (atomicAdd(&w.counters[kP2GDone], 1) == (int)(gridDim.x * kP2GWarps) - 1) {
+      w.counters[kP2GQueue] = 0;
+      w.counters[kP2GDone] = 0;
+    }
+  }
 }
 
 // --------------------------------------------------------------- grid ----
@@ -704,17 +868,21 @@ __global__ __launch_bounds__(kG2PThreads, 8) void k_g2p(const MpmParams P, const
 // scatters straight to the grid with global atomics.  The new positions are
 // binned for the next substep, as in G2P.
 
+__device__ __forceinline__ float4 f4add(float4 a, float4 b) {
+  return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+}
+
 constexpr int kFusedTileW = 8;
 constexpr int kFusedTileN = kFusedTileW * kFusedTileW * kFusedTileW;
 
 template <bool Q>
-__global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_g2p2g(const MpmParams P, const Ws w,
+__global__ __launch_bounds__(kFusedThreads, MPM_FUSED_MIN_CTAS) void k_g2p2g(const MpmParams P, const Ws w,
                                                                          const float *__restrict__ cur,
                                                                          float *__restrict__ nxt, int64_t cap,
                                                                          float dt, int64_t first_new,
                                                                          float *maxv_out) {
   __shared__ float4 vt[kTileN];
-  __shared__ float4 tiles[kP2GWarps][kFusedTileN];
+  __shared__ float4 tiles[kFusedWarps][kFusedTileN];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   float4 *tile = tiles[warp];
   const int nitems = (int)min((int64_t)w.counters[2], w.items_cap);
@@ -737,7 +905,7 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_g2p2g(const M
     }
     for (int t = lane; t < kFusedTileN; t += 32) tile[t] = make_float4(0.f, 0.f, 0.f, 0.f);
     __syncthreads();
-    for (int j0 = start + warp * 32; j0 < end; j0 += kP2GThreads) {
+    for (int j0 = start + warp * 32; j0 < end; j0 += kFusedThreads) {
       const int j = j0 + lane;
       bool active = j < end;
       int64_t i = active ? w.pid[j] : 0;
@@ -895,7 +1063,7 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_g2p2g(const M
     for (int t = threadIdx.x; t < kFusedTileN; t += blockDim.x) {
       float4 g = tiles[0][t];
 #pragma unroll
-      for (int wq = 1; wq < kP2GWarps; ++wq) g = f4add(g, tiles[wq][t]);
+      for (int wq = 1; wq < kFusedWarps; ++wq) g = f4add(g, tiles[wq][t]);
       if (g.x != 0.0f) {
         const int tx = t / 64, ty = (t / 8) % 8, tz = t % 8;
         const int gx = bx * 4 - 1 + tx, gy = by * 4 - 1 + ty, gz = bz * 4 - 1 + tz;
@@ -941,6 +1109,65 @@ __global__ void k_gather_rows(const float *__restrict__ ps, int64_t cap, int64_t
 
 // ------------------------------------------------------------ host side --
 
+// cuTensorMapEncodeTiled, looked up once through the runtime (no link
+// against the driver library)
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+
+// Tensor map of the first `rows` rows of a state buffer: a 2-D float32
+// tensor of cap x rows elements (row stride cap), boxes of 32 slots x rows.
+static bool rows_tensor_map(CUtensorMap *map, const float *state, int64_t cap, int rows) {
+  const EncodeTiledFn fn = encode_tiled();
+  if (!fn) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)cap, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)cap * sizeof(float)};
+  const cuuint32_t box[2] = {32u, (cuuint32_t)rows};
+  const cuuint32_t elem[2] = {1u, 1u};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(state), dims, strides, box, elem,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <bool HAS_EP, bool BATCH, bool Q>
+static int launch_p2g(int ctas, cudaStream_t s, const MpmParams &p, const MpmParams *tab, const Ws &w,
+                      const float *cur, float *nxt, int64_t cap, int64_t n, float dt) {
+  if (n <= 0) return MPM_OK;
+  CUtensorMap map;
+  if (!rows_tensor_map(&map, cur, cap, P2GRows<Q, HAS_EP>::N)) return MPM_E_CUDA;
+  k_p2g<HAS_EP, BATCH, Q><<<ctas, kP2GThreads, kP2GSmem, s>>>(p, tab, w, map, cur, nxt, cap, n, dt);
+  return MPM_OK;
+}
+
+template <bool HAS_EP, bool BATCH, bool Q>
+static int p2g_occupancy() {
+  auto k = k_p2g<HAS_EP, BATCH, Q>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kP2GSmem);
+  int c = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k, kP2GThreads, kP2GSmem);
+  return c > 0 ? c : 1;
+}
+
+// P2G stages 128-byte row segments with bulk copies: row starts must be
+// 16-byte aligned and whole 32-slot steps must lie inside the buffers.
+static bool p2g_rows_ok(const void *cur, int64_t cap) {
+  return cap % 32 == 0 && ((uintptr_t)cur & 15u) == 0;
+}
+
 struct DevInfo {
   int sms = 0;
   int p2g_ctas = 0, p2g_ep_ctas = 0, g2p_ctas = 0, g2p2g_ctas = 0;
@@ -960,18 +1187,18 @@ static const DevInfo *dev_info() {
     int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return nullptr;
     int a = 0, b = 0, c = 0, a2 = 0, b2 = 0, c2 = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_p2g<false, false, false>, kP2GThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_p2g<true, false, false>, kP2GThreads, 0);
+    a = p2g_occupancy<false, false, false>();
+    b = p2g_occupancy<true, false, false>();
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k_g2p<false, false, kBinKeep>, kG2PThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a2, k_p2g<false, true, false>, kP2GThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b2, k_p2g<true, true, false>, kP2GThreads, 0);
+    a2 = p2g_occupancy<false, true, false>();
+    b2 = p2g_occupancy<true, true, false>();
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c2, k_g2p<true, false, kBinPlain>, kG2PThreads, 0);
     int f = 0, aq = 0, bq = 0, cq = 0, fq = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, k_g2p2g<false>, kP2GThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&aq, k_p2g<false, false, true>, kP2GThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bq, k_p2g<true, false, true>, kP2GThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, k_g2p2g<false>, kFusedThreads, 0);
+    aq = p2g_occupancy<false, false, true>();
+    bq = p2g_occupancy<true, false, true>();
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cq, k_g2p<false, true, kBinKeep>, kG2PThreads, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fq, k_g2p2g<true>, kP2GThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fq, k_g2p2g<true>, kFusedThreads, 0);
     d.g2p2g_ctas = sms * (f > 0 ? f : 1);
     d.p2g_q_ctas = sms * (aq > 0 ? aq : 1);
     d.p2g_ep_q_ctas = sms * (bq > 0 ? bq : 1);
@@ -986,6 +1213,16 @@ static const DevInfo *dev_info() {
     d.sms = sms;
   }
   return &d;
+}
+
+// P2G of a single scene in the parameters' storage layout
+static int launch_p2g_single(const DevInfo *di, cudaStream_t s, const MpmParams &p, const Ws &w, const float *cur,
+                             float *nxt, int64_t cap, int64_t n, float dt) {
+  if (p.quant)
+    return p.has_Ep ? launch_p2g<true, false, true>(di->p2g_ep_q_ctas, s, p, nullptr, w, cur, nxt, cap, n, dt)
+                    : launch_p2g<false, false, true>(di->p2g_q_ctas, s, p, nullptr, w, cur, nxt, cap, n, dt);
+  return p.has_Ep ? launch_p2g<true, false, false>(di->p2g_ep_ctas, s, p, nullptr, w, cur, nxt, cap, n, dt)
+                  : launch_p2g<false, false, false>(di->p2g_ctas, s, p, nullptr, w, cur, nxt, cap, n, dt);
 }
 
 static bool params_ok(const MpmParams *p) {
@@ -1087,23 +1324,14 @@ int mpm_bin_finalize(const MpmParams *p, void *ws, int64_t cap, int64_t n, void 
 
 int mpm_p2g(const MpmParams *p, void *ws, int64_t cap, int64_t n, const float *cur, float *nxt, float dt,
             void *stream) {
-  if (!params_ok(p) || !ws || !cur || !nxt || n < 0 || n > cap) return MPM_E_INVALID;
+  if (!params_ok(p) || !ws || !cur || !nxt || n < 0 || n > cap || !p2g_rows_ok(cur, cap)) return MPM_E_INVALID;
   const DevInfo *di = dev_info();
   if (!di) return MPM_E_CUDA;
   Ws w;
   ws_layout(*p, cap, (char *)ws, &w);
   cudaStream_t s = (cudaStream_t)stream;
-  if (p->quant) {
-    if (p->has_Ep)
-      k_p2g<true, false, true><<<di->p2g_ep_q_ctas, kP2GThreads, 0, s>>>(*p, nullptr, w, cur, nxt, cap, dt);
-    else
-      k_p2g<false, false, true><<<di->p2g_q_ctas, kP2GThreads, 0, s>>>(*p, nullptr, w, cur, nxt, cap, dt);
-  } else if (p->has_Ep) {
-    k_p2g<true, false, false><<<di->p2g_ep_ctas, kP2GThreads, 0, s>>>(*p, nullptr, w, cur, nxt, cap, dt);
-  } else {
-    k_p2g<false, false, false><<<di->p2g_ctas, kP2GThreads, 0, s>>>(*p, nullptr, w, cur, nxt, cap, dt);
-  }
-  return last_error();
+  const int rc = launch_p2g_single(di, s, *p, w, cur, nxt, cap, n, dt);
+  return rc ? rc : last_error();
 }
 
 int mpm_grid_update(const MpmParams *p, void *ws, int64_t cap, float dt, void *stream) {
@@ -1167,10 +1395,10 @@ int mpm_g2p2g_substep(const MpmParams *p, void *ws, int64_t cap, int64_t n, cons
   Ws w;
   ws_layout(*p, cap, (char *)ws, &w);
   if (p->quant)
-    k_g2p2g<true><<<di->g2p2g_q_ctas, kP2GThreads, 0, (cudaStream_t)stream>>>(*p, w, cur, nxt, cap, dt, first_new,
+    k_g2p2g<true><<<di->g2p2g_q_ctas, kFusedThreads, 0, (cudaStream_t)stream>>>(*p, w, cur, nxt, cap, dt, first_new,
                                                                               maxv_out);
   else
-    k_g2p2g<false><<<di->g2p2g_ctas, kP2GThreads, 0, (cudaStream_t)stream>>>(*p, w, cur, nxt, cap, dt, first_new,
+    k_g2p2g<false><<<di->g2p2g_ctas, kFusedThreads, 0, (cudaStream_t)stream>>>(*p, w, cur, nxt, cap, dt, first_new,
                                                                              maxv_out);
   rc = last_error();
   if (rc) return rc;
@@ -1181,6 +1409,7 @@ int mpm_g2p2g_substep(const MpmParams *p, void *ws, int64_t cap, int64_t n, cons
 
 int mpm_substep(const MpmParams *p, void *ws, int64_t cap, int64_t n, const float *cur, float *nxt, float dt,
                 float *maxv_out, void *stream) {
+  if (!cur || !p2g_rows_ok(cur, cap)) return MPM_E_INVALID;  // checked before any device work
   int rc = mpm_bin_finalize(p, ws, cap, n, stream);
   if (rc) return rc;
   rc = mpm_p2g(p, ws, cap, n, cur, nxt, dt, stream);
@@ -1215,7 +1444,8 @@ int mpm_batch_bin_count(const MpmParams *p, const MpmParams *scenes, void *ws, i
 
 int mpm_batch_substep(const MpmParams *p, const MpmParams *scenes, void *ws, int64_t cap, int64_t n,
                       const float *cur, float *nxt, float *maxv_out, void *stream) {
-  if (!batch_ok(p) || !scenes || !ws || !cur || !nxt || n < 0 || n > cap) return MPM_E_INVALID;
+  if (!batch_ok(p) || !scenes || !ws || !cur || !nxt || n < 0 || n > cap || !p2g_rows_ok(cur, cap))
+    return MPM_E_INVALID;
   int rc = mpm_bin_finalize(p, ws, cap, n, stream);
   if (rc) return rc;
   const DevInfo *di = dev_info();
@@ -1223,10 +1453,9 @@ int mpm_batch_substep(const MpmParams *p, const MpmParams *scenes, void *ws, int
   Ws w;
   ws_layout(*p, cap, (char *)ws, &w);
   cudaStream_t s = (cudaStream_t)stream;
-  if (p->has_Ep)
-    k_p2g<true, true, false><<<di->p2g_ep_b_ctas, kP2GThreads, 0, s>>>(*p, scenes, w, cur, nxt, cap, 0.0f);
-  else
-    k_p2g<false, true, false><<<di->p2g_b_ctas, kP2GThreads, 0, s>>>(*p, scenes, w, cur, nxt, cap, 0.0f);
+  rc = p->has_Ep ? launch_p2g<true, true, false>(di->p2g_ep_b_ctas, s, *p, scenes, w, cur, nxt, cap, n, 0.0f)
+                 : launch_p2g<false, true, false>(di->p2g_b_ctas, s, *p, scenes, w, cur, nxt, cap, n, 0.0f);
+  if (rc) return rc;
   k_grid<true><<<di->sms * 8, 256, 0, s>>>(*p, scenes, w, 0.0f);
   k_g2p<true, false, kBinPlain><<<di->g2p_b_ctas, kG2PThreads, 0, s>>>(*p, scenes, w, nxt, cap, 0.0f, maxv_out);
   return last_error();
@@ -1238,6 +1467,7 @@ int mpm_substep_noalloc(const MpmParams *p, int64_t cap, int64_t n, const float 
   if (n > kStaticMaxParticles) return MPM_E_CAPACITY;
   const size_t bytes = ws_layout(*p, kStaticMaxParticles, nullptr, nullptr);
   if (bytes > kStaticScratchBytes) return MPM_E_CAPACITY;
+  if (!p2g_rows_ok(cur, cap)) return MPM_E_INVALID;
   const DevInfo *di = dev_info();
   if (!di) return MPM_E_CUDA;
   void *base = nullptr;
@@ -1258,10 +1488,8 @@ int mpm_substep_noalloc(const MpmParams *p, int64_t cap, int64_t n, const float 
     k_pb_levels<<<di->sms * 8, 256, 0, s>>>(*p, w, kStaticMaxParticles);
     k_scatter<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(*p, w, n);
     k_cell_clear<<<di->sms * 8, 256, 0, s>>>(*p, w);
-    if (p->has_Ep)
-      k_p2g<true, false, false><<<di->p2g_ep_ctas, kP2GThreads, 0, s>>>(*p, nullptr, w, cur, nxt, cap, dt);
-    else
-      k_p2g<false, false, false><<<di->p2g_ctas, kP2GThreads, 0, s>>>(*p, nullptr, w, cur, nxt, cap, dt);
+    const int rc_p = launch_p2g_single(di, s, *p, w, cur, nxt, cap, n, dt);
+    if (rc_p) return rc_p;
     k_grid<false><<<di->sms * 8, 256, 0, s>>>(*p, nullptr, w, dt);
     // the next call bins from scratch, so G2P skips the binning
     k_g2p<false, false, kBinNone><<<di->g2p_ctas, kG2PThreads, 0, s>>>(*p, nullptr, w, nxt, cap, dt, maxv_out);

@@ -637,6 +637,8 @@ class MPMSolver:
                 msgs.append("non-finite particle positions")
             if st & _lib.STATUS_TABLE_OVERFLOW:
                 msgs.append("binning tables inconsistent (stale particle binning)")
+            if st & _lib.STATUS_TIMEOUT:
+                msgs.append("a kernel gave up waiting for staged particle data")
             raise MPMError("MPM device status: " + "; ".join(msgs))
 
     def _launch_substep(self, dt: float, maxv_slot: int):

@@ -47,6 +47,8 @@ constexpr int kFusedWarps = kFusedThreads / 32;
 constexpr int kG2PThreads = 128;
 
 
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+
 // ------------------------------------------------------------ binning ----
 
 // kNeighbourMask[need]: bits of all neighbour offsets d (dx*4+dy*2+dz) whose
@@ -418,7 +420,7 @@ __global__ __launch_bounds__(256) void k_cell_clear(const MpmParams P, const Ws 
 // atomics.  Lanes of a step hold distinct cells (rank-major order), so the 27
 // node updates of a pass never collide; particles that moved into a shared
 // cell are found with __match_any_sync and scatter in later passes.  Steps
-// are taken from a queue in guided runs of consecutive steps.
+// are taken from a guided queue in runs of consecutive steps.
 
 constexpr int kP2GWarps = 4;
 // P2G CTAs per SM the register budget is sized for (168 registers at 3; 4 would
@@ -427,7 +429,6 @@ constexpr int kP2GWarps = 4;
 #define MPM_P2G_MIN_CTAS 3
 #endif
 constexpr int kP2GThreads = kP2GWarps * 32;
-constexpr int kP2GRun = 16;                    // longest run of steps per queue grab
 constexpr int kP2GQueue = 5, kP2GDone = 6;     // counters[]: run queue, warps done
 constexpr int kP2GTileW = 8;                   // tile nodes per axis
 // tile index = tx * 76 + ty * 9 + tz: the x stride is 4 mod 8, so the 8 lanes
@@ -474,24 +475,38 @@ __device__ __forceinline__ void p2g_tile_flush(const MpmParams &P, const Ws &w, 
   __syncwarp();
 }
 
-// The next step of this warp (warp-uniform; -1 when the queue is empty).
-// Lane 0 keeps the cursor (q_next, q_end) of its current run.  Runs are
-// guided: a grab takes about a (2 * warps)-th of the steps left, at most
-// kP2GRun, so the last grabs are single steps and warps finish together.
-__device__ __forceinline__ int p2g_next_step(const Ws &w, int lane, int nsteps, int nwarps, int &q_next,
-                                             int &q_end) {
+// The next step of this warp (warp-uniform; -1 when the queue is empty)
+// from the step queue in counters[q].  Lane 0 keeps the cursor (q_next,
+// q_end) of its current run.  Runs are guided: a grab takes about a
+// (2 * warps)-th of the steps left, at most kStepRun, so the last grabs are
+// single steps and warps finish together.
+constexpr int kStepRun = 16;
+__device__ __forceinline__ int step_queue_next(const Ws &w, int q, int lane, int nsteps, int nwarps, int &q_next,
+                                               int &q_end) {
   int g = -1;
   if (lane == 0) {
     if (q_next >= q_end) {
-      const int seen = *(volatile const int *)&w.counters[kP2GQueue];
-      const int len = max(1, min(kP2GRun, (nsteps - seen) / (2 * nwarps)));
-      const int r = atomicAdd(&w.counters[kP2GQueue], len);
+      const int seen = *(volatile const int *)&w.counters[q];
+      const int len = max(1, min(kStepRun, (nsteps - seen) / (2 * nwarps)));
+      const int r = atomicAdd(&w.counters[q], len);
       q_next = min(r, nsteps);
       q_end = min(r + len, nsteps);
     }
     if (q_next < q_end) g = q_next++;
   }
   return __shfl_sync(0xffffffffu, g, 0);
+}
+
+// The last warp of the launch to finish resets the queue counters[q] (and
+// the done counter counters[d]), so the kernel can run again.
+__device__ __forceinline__ void step_queue_done(const Ws &w, int q, int d, int lane, int nwarps) {
+  if (lane == 0) {
+    __threadfence();
+    if (atomicAdd(&w.counters[d], 1) == nwarps - 1) {
+      w.counters[q] = 0;
+      w.counters[d] = 0;
+    }
+  }
 }
 
 // Stages step g: one tensor-map box of NR rows x 32 slots and the 32 sorted
@@ -532,7 +547,7 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_p2g(const Mpm
   // step's copy is issued into the buffer and lands while this step computes.
   int q_next = 0, q_end = 0;  // lane 0's cursor in the run queue
   uint32_t parity = 0u;
-  int g0 = p2g_next_step(w, lane, nsteps, nwarps, q_next, q_end);
+  int g0 = step_queue_next(w, kP2GQueue, lane, nsteps, nwarps, q_next, q_end);
   if (g0 >= 0) p2g_issue<NR>(sm, rows_map, w, g0, lane);
   bool anchored = false;
   int o[3] = {0, 0, 0};
@@ -566,7 +581,7 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_p2g(const Mpm
     const int64_t j = __float_as_int(sb[NR * 32 + lane]);
     __syncwarp();
     // the buffer is free: stage the next step into it
-    const int g1 = p2g_next_step(w, lane, nsteps, nwarps, q_next, q_end);
+    const int g1 = step_queue_next(w, kP2GQueue, lane, nsteps, nwarps, q_next, q_end);
     if (g1 >= 0) p2g_issue<NR>(sm, rows_map, w, g1, lane);
 
     if (act && (j < 0 || j >= n)) {
@@ -696,14 +711,7 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_p2g(const Mpm
   }
   if (anchored) p2g_tile_flush(P, w, sm.tile, o, lane);
   set_status(w, bad);
-  // the last warp to finish resets the queue, so the kernel can run again
-  if (lane == 0) {
-    __threadfence();
-    if (atomicAdd(&w.counters[kP2GDone], 1) == (int)(gridDim.x * kP2GWarps) - 1) {
-      w.counters[kP2GQueue] = 0;
-      w.counters[kP2GDone] = 0;
-    }
-  }
+  step_queue_done(w, kP2GQueue, kP2GDone, lane, nwarps);
 }
 
 // --------------------------------------------------------------- grid ----
@@ -776,36 +784,33 @@ __global__ __launch_bounds__(kG2PThreads, 8) void k_g2p(const MpmParams P, const
         bad |= MPM_STATUS_TABLE_OVERFLOW;
         continue;
       }
-      // Gather, :711-721, in separable form: with t = w g,
-      //   v = sum t,  C = 4 inv_dx (sum t (x) off - v (x) fx)
+      // Gather, :711-721, in separable form.  Along each z-line (a, b) of
+      // the stencil, T = sum_c w_c^z g and U = sum_c c w_c^z g; then with
+      // W = w_a^x w_b^y:  v = sum W T,  C = 4 inv_dx (S - v (x) fx) where the
+      // columns of S are sum a W T, sum b W T, sum W U.
       float nv[3] = {0.f, 0.f, 0.f}, sa[3] = {0.f, 0.f, 0.f}, sb[3] = {0.f, 0.f, 0.f},
             sc[3] = {0.f, 0.f, 0.f};
       const int base_node = (lx * kTileW + ly) * kTileW + lz;
+      const float wz0 = wt[0][2], wz1 = wt[1][2], wz2x2 = 2.0f * wt[2][2], wz2 = wt[2][2];
 #pragma unroll
       for (int a = 0; a < 3; ++a)
 #pragma unroll
         for (int bb = 0; bb < 3; ++bb) {
-          const float wab = wt[a][0] * wt[bb][1];
-          float T[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            const float4 g = vt[base_node + (a * kTileW + bb) * kTileW + c];
-            const float wgt = wab * wt[c][2];
-            const float t0 = wgt * g.x, t1 = wgt * g.y, t2 = wgt * g.z;
-            T[0] += t0;
-            T[1] += t1;
-            T[2] += t2;
-            if (c > 0) {
-              sc[0] = fmaf((float)c, t0, sc[0]);
-              sc[1] = fmaf((float)c, t1, sc[1]);
-              sc[2] = fmaf((float)c, t2, sc[2]);
-            }
-          }
+          const float4 *line = vt + base_node + (a * kTileW + bb) * kTileW;
+          const float4 g0 = line[0], g1 = line[1], g2 = line[2];
+          const float2 T01 = __ffma2_rn(f2(wz2, wz2), f2(g2.x, g2.y),
+                                        __ffma2_rn(f2(wz1, wz1), f2(g1.x, g1.y), __fmul2_rn(f2(wz0, wz0), f2(g0.x, g0.y))));
+          const float T2 = fmaf(wz2, g2.z, fmaf(wz1, g1.z, wz0 * g0.z));
+          const float2 U01 = __ffma2_rn(f2(wz2x2, wz2x2), f2(g2.x, g2.y), __fmul2_rn(f2(wz1, wz1), f2(g1.x, g1.y)));
+          const float U2 = fmaf(wz2x2, g2.z, wz1 * g1.z);
+          const float W = wt[a][0] * wt[bb][1];
+          const float T[3] = {T01.x, T01.y, T2}, U[3] = {U01.x, U01.y, U2};
 #pragma unroll
           for (int r = 0; r < 3; ++r) {
-            nv[r] += T[r];
-            if (a > 0) sa[r] = fmaf((float)a, T[r], sa[r]);
-            if (bb > 0) sb[r] = fmaf((float)bb, T[r], sb[r]);
+            nv[r] = fmaf(W, T[r], nv[r]);
+            sc[r] = fmaf(W, U[r], sc[r]);
+            if (a > 0) sa[r] = fmaf((float)a * W, T[r], sa[r]);
+            if (bb > 0) sb[r] = fmaf((float)bb * W, T[r], sb[r]);
           }
         }
       float nC[3][3];

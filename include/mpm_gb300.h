@@ -171,6 +171,23 @@ int mpm_g2p(const MpmParams *p, void *ws, int64_t cap, int64_t n, float *nxt, fl
 int mpm_substep(const MpmParams *p, void *ws, int64_t cap, int64_t n, const float *cur, float *nxt,
                 float dt, float *maxv_out, void *stream);
 
+/* `count` plain substeps of one frame: the substep loop of step(),
+ * engine/mpm_solver.py:748-799, with the same per-substep arithmetic as
+ * mpm_substep.  Every `resort` substeps (and at the first) the particles are
+ * re-sorted by grid block (finalize + p2g into the other buffer); between
+ * sorts the G2P of one substep and the P2G of the next run as one kernel in
+ * place, with the grid's active blocks marked by the particles as they
+ * scatter.  The last substep's G2P bins the state for the next call.
+ * Preconditions: the workspace holds the binning counts of the state in `a`
+ * (mpm_bin_count of every particle, or a previous mpm_substep / mpm_g2p /
+ * mpm_frame on it); both buffers satisfy mpm_p2g's layout rules; no
+ * quantized state, no batch (n_scenes == 0).  `maxv` receives the max |v|
+ * after each substep (count floats).  On return `*in_b` is 1 when the state
+ * ends in `b`, 0 when in `a`.  No single counterpart in the reference, whose
+ * loop launches the four kernels of each substep separately. */
+int mpm_frame(const MpmParams *p, void *ws, int64_t cap, int64_t n, float *a, float *b, float dt, int32_t count,
+              int32_t resort, float *maxv, int32_t *in_b, void *stream);
+
 /* One substep of the fused G2P2G mode (MPMSolver(use_g2p2g=True),
  * engine/mpm_solver.py:363-485 and :773-787): G2P from the grid velocities of
  * the previous substep, advection, the constitutive update and P2G at the new

@@ -25,7 +25,8 @@ enum Row : int {
 
 // Device pointers into the caller-owned workspace.
 struct Ws {
-  int32_t *counters;  // [32]: 0 #pblocks, 1 #gblocks, 2 #items, 3 status, 4 #binned
+  int32_t *counters;  // [32]: 0 #pblocks, 1 #gblocks, 2 #items, 3 status, 4 #binned, 5-8 work queues,
+                      // 16-21 particle bounding box after G2P (order-preserving float keys: min x,y,z, max x,y,z)
   int32_t *blk_flag;  // [nblk]
   int32_t *blk_slot;  // [nblk] window block -> compact particle-block index
   int32_t *pblocks;   // [nblk] compact particle-active blocks (ascending)
@@ -139,6 +140,14 @@ __device__ __forceinline__ Base particle_base(const MpmParams &P, float x0, floa
     r.fx[d] = __fsub_rn(s, (float)g);
   }
   return r;
+}
+
+// Bounding-box slots of counters[] and the order-preserving int32 key of a
+// float (monotonic: a < b iff key(a) < key(b) for finite values).
+constexpr int kBoxMin = 16, kBoxMax = 19;
+__device__ __forceinline__ int float_key_i32(float f) {
+  const int b = __float_as_int(f);
+  return b >= 0 ? b : b ^ 0x7FFFFFFF;
 }
 
 __device__ __forceinline__ void set_status(const Ws &w, uint32_t bits) {

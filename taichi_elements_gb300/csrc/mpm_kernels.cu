@@ -30,6 +30,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cstddef>
 #include <mutex>
 
 #include "mpm_common.cuh"
@@ -241,6 +242,11 @@ __global__ __launch_bounds__(256) void k_flags_write(const MpmParams P, const Ws
     w.counters[1] = og;
     w.counters[2] = 0;
     w.counters[4] = 0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {  // the next G2P's bounding box starts empty
+      w.counters[kBoxMin + d] = float_key_i32(INFINITY);
+      w.counters[kBoxMax + d] = float_key_i32(-INFINITY);
+    }
   }
 }
 
@@ -458,21 +464,127 @@ __device__ __forceinline__ int p2g_tile_index(int tx, int ty, int tz) {
 }
 
 // Flushes the warp's tile anchored at node o (window-relative) to the grid
-// and clears it.
+// and clears it.  MARK: also flag the 4^3 blocks that received momentum
+// (bit 0 of blk_flag), which then make the grid-active list of a substep
+// without binning.
+template <bool MARK = false>
 __device__ __forceinline__ void p2g_tile_flush(const MpmParams &P, const Ws &w, float4 *tile, const int (&o)[3],
                                                int lane) {
+  uint32_t touched = 0u;  // bit (bx * 3 + by) * 3 + bz over the <= 3^3 blocks the window overlaps
   for (int t = lane; t < kP2GTileW * kP2GTileW * kP2GTileW; t += 32) {
     const int tx = t >> 6, ty = (t >> 3) & 7, tz = t & 7;
     float4 &nd = tile[p2g_tile_index(tx, ty, tz)];
     const float4 g = nd;
     if (g.x != 0.0f) {
       const int gx = o[0] + tx, gy = o[1] + ty, gz = o[2] + tz;
-      if (gx < P.win_nb[0] * 4 && gy < P.win_nb[1] * 4 && gz < P.win_nb[2] * 4)
+      if (gx < P.win_nb[0] * 4 && gy < P.win_nb[1] * 4 && gz < P.win_nb[2] * 4) {
         atomicAdd(&w.grid_mom[node_addr(P, gx, gy, gz)], g);
+        if (MARK)
+          touched |= 1u << ((((gx >> 2) - (o[0] >> 2)) * 3 + ((gy >> 2) - (o[1] >> 2))) * 3 + ((gz >> 2) - (o[2] >> 2)));
+      }
       nd = make_float4(0.f, 0.f, 0.f, 0.f);
     }
   }
+  if (MARK) {
+    touched = __reduce_or_sync(0xffffffffu, touched);
+    if (lane < 27 && ((touched >> lane) & 1u)) {
+      const int bx = (o[0] >> 2) + lane / 9, by = (o[1] >> 2) + (lane / 3) % 3, bz = (o[2] >> 2) + lane % 3;
+      atomicOr(&w.blk_flag[block_linear(P, bx, by, bz)], 1);
+    }
+  }
   __syncwarp();
+}
+
+// The APIC scatter (engine/mpm_solver.py:576-584) of one warp step into the
+// warp's tile: node value = w * (m v + A (off - fx) dx) = w * ((m, q) +
+// a Ax + b Ay + c Az), q = m v - A fx dx, Ax..Az the columns of A dx.  The
+// tile is anchored at the step's base cells (see k_p2g); a particle outside a
+// fresh anchor scatters with global atomics.  MARK: flag the blocks that
+// receive momentum (see p2g_tile_flush).
+template <bool MARK>
+__device__ __forceinline__ void p2g_scatter_step(const MpmParams &P, const Ws &w, float4 *tile, int (&o)[3],
+                                                 bool &anchored, bool act, const Base &bs, const float (&wt)[3][3],
+                                                 float mass, const float (&q)[3], const float (&adx)[3][3],
+                                                 int lane) {
+  // anchor the tile: all base cells within [o, o + 5]
+  int lo[3], hi[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    lo[d] = __reduce_min_sync(0xffffffffu, act ? bs.b[d] : INT32_MAX);
+    hi[d] = __reduce_max_sync(0xffffffffu, act ? bs.b[d] : INT32_MIN);
+  }
+  if (__any_sync(0xffffffffu, act)) {
+    const bool fits = anchored && lo[0] >= o[0] && lo[1] >= o[1] && lo[2] >= o[2] &&
+                      hi[0] <= o[0] + kP2GTileW - 3 && hi[1] <= o[1] + kP2GTileW - 3 &&
+                      hi[2] <= o[2] + kP2GTileW - 3;
+    if (!fits) {
+      if (anchored) p2g_tile_flush<MARK>(P, w, tile, o, lane);
+      // one cell of slack below: the steps of one block of the previous
+      // binning have base cells in [B - 1, B + 4] (B the block's first
+      // cell), and the first step's smallest is usually B
+#pragma unroll
+      for (int d = 0; d < 3; ++d) o[d] = hi[d] - lo[d] <= kP2GTileW - 4 ? max(lo[d] - 1, 0) : lo[d];
+      anchored = true;
+    }
+  }
+  const int tx0 = bs.b[0] - o[0], ty0 = bs.b[1] - o[1], tz0 = bs.b[2] - o[2];
+  const bool inwin = act && (unsigned)tx0 <= kP2GTileW - 3 && (unsigned)ty0 <= kP2GTileW - 3 &&
+                     (unsigned)tz0 <= kP2GTileW - 3;
+  if (act && !inwin) {  // rare: straight to the grid
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int bb = 0; bb < 3; ++bb)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const int gx = bs.b[0] + a, gy = bs.b[1] + bb, gz = bs.b[2] + c;
+          if (gx >= P.win_nb[0] * 4 || gy >= P.win_nb[1] * 4 || gz >= P.win_nb[2] * 4) continue;
+          const float wgt = wt[a][0] * wt[bb][1] * wt[c][2];
+          float4 g;
+          g.x = wgt * mass;
+          g.y = wgt * (q[0] + adx[0][0] * (float)a + adx[0][1] * (float)bb + adx[0][2] * (float)c);
+          g.z = wgt * (q[1] + adx[1][0] * (float)a + adx[1][1] * (float)bb + adx[1][2] * (float)c);
+          g.w = wgt * (q[2] + adx[2][0] * (float)a + adx[2][1] * (float)bb + adx[2][2] * (float)c);
+          atomicAdd(&w.grid_mom[node_addr(P, gx, gy, gz)], g);
+          if (MARK && wgt != 0.0f) atomicOr(&w.blk_flag[block_linear(P, gx >> 2, gy >> 2, gz >> 2)], 1);
+        }
+  }
+  // tile scatter: one pass per set of lanes with distinct base cells
+  const int cell = inwin ? p2g_tile_index(tx0, ty0, tz0) : -1 - lane;
+  const unsigned peers = __match_any_sync(0xffffffffu, cell);
+  const int round_of_lane = __popc(peers & ((1u << lane) - 1u));
+  const int base_node = inwin ? cell : 0;
+  for (int round = 0;; ++round) {
+    const bool mine = inwin && round_of_lane == round;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int bb = 0; bb < 3; ++bb) {
+        const float wab = wt[a][0] * wt[bb][1];
+        const float2 p0 = make_float2(mass, fmaf(adx[0][1], (float)bb, fmaf(adx[0][0], (float)a, q[0])));
+        const float2 p1 = make_float2(fmaf(adx[1][1], (float)bb, fmaf(adx[1][0], (float)a, q[1])),
+                                      fmaf(adx[2][1], (float)bb, fmaf(adx[2][0], (float)a, q[2])));
+        const float2 dz0 = make_float2(0.0f, adx[0][2]), dz1 = make_float2(adx[1][2], adx[2][2]);
+        float2 t0 = p0, t1 = p1;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          // unconditional read and arithmetic, predicated store only
+          const float wgt = wab * wt[c][2];
+          const float2 w2 = make_float2(wgt, wgt);
+          float4 *nd = tile + base_node + a * kP2GTileSX + bb * kP2GTileSY + c;
+          float4 g = *nd;
+          const float2 g01 = __ffma2_rn(w2, t0, make_float2(g.x, g.y));
+          const float2 g23 = __ffma2_rn(w2, t1, make_float2(g.z, g.w));
+          if (mine) *nd = make_float4(g01.x, g01.y, g23.x, g23.y);
+          __syncwarp();
+          if (c < 2) {
+            t0 = __fadd2_rn(t0, dz0);
+            t1 = __fadd2_rn(t1, dz1);
+          }
+        }
+      }
+    if (!__any_sync(0xffffffffu, inwin && round_of_lane > round)) break;
+  }
 }
 
 // The next step of this warp (warp-uniform; -1 when the queue is empty)
@@ -628,88 +740,10 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_p2g(const Mpm
 #pragma unroll
         for (int c = 0; c < 3; ++c) adx[r][c] = out.affine[r][c] * S.dx;
     }
-    // anchor the tile: all base cells within [o, o + 5]
-    int lo[3], hi[3];
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      lo[d] = __reduce_min_sync(0xffffffffu, act ? bs.b[d] : INT32_MAX);
-      hi[d] = __reduce_max_sync(0xffffffffu, act ? bs.b[d] : INT32_MIN);
-    }
-    const bool any = __any_sync(0xffffffffu, act);
-    if (any) {
-      const bool fits = anchored && lo[0] >= o[0] && lo[1] >= o[1] && lo[2] >= o[2] &&
-                        hi[0] <= o[0] + kP2GTileW - 3 && hi[1] <= o[1] + kP2GTileW - 3 &&
-                        hi[2] <= o[2] + kP2GTileW - 3;
-      if (!fits) {
-        if (anchored) p2g_tile_flush(P, w, sm.tile, o, lane);
-        // one cell of slack below: the steps of one block of the previous
-        // binning have base cells in [B - 1, B + 4] (B the block's first
-        // cell), and the first step's smallest is usually B
-#pragma unroll
-        for (int d = 0; d < 3; ++d) o[d] = hi[d] - lo[d] <= kP2GTileW - 4 ? max(lo[d] - 1, 0) : lo[d];
-        anchored = true;
-      }
-    }
-    const int tx0 = bs.b[0] - o[0], ty0 = bs.b[1] - o[1], tz0 = bs.b[2] - o[2];
-    const bool inwin = act && (unsigned)tx0 <= kP2GTileW - 3 && (unsigned)ty0 <= kP2GTileW - 3 &&
-                       (unsigned)tz0 <= kP2GTileW - 3;
-    if (act && !inwin) {  // rare: straight to the grid
-#pragma unroll
-      for (int a = 0; a < 3; ++a)
-#pragma unroll
-        for (int bb = 0; bb < 3; ++bb)
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            const int gx = bs.b[0] + a, gy = bs.b[1] + bb, gz = bs.b[2] + c;
-            if (gx >= P.win_nb[0] * 4 || gy >= P.win_nb[1] * 4 || gz >= P.win_nb[2] * 4) continue;
-            const float wgt = wt[a][0] * wt[bb][1] * wt[c][2];
-            float4 g;
-            g.x = wgt * mass;
-            g.y = wgt * (q[0] + adx[0][0] * (float)a + adx[0][1] * (float)bb + adx[0][2] * (float)c);
-            g.z = wgt * (q[1] + adx[1][0] * (float)a + adx[1][1] * (float)bb + adx[1][2] * (float)c);
-            g.w = wgt * (q[2] + adx[2][0] * (float)a + adx[2][1] * (float)bb + adx[2][2] * (float)c);
-            atomicAdd(&w.grid_mom[node_addr(P, gx, gy, gz)], g);
-          }
-    }
-    // tile scatter: one pass per set of lanes with distinct base cells
-    const int cell = inwin ? p2g_tile_index(tx0, ty0, tz0) : -1 - lane;
-    const unsigned peers = __match_any_sync(0xffffffffu, cell);
-    const int round_of_lane = __popc(peers & ((1u << lane) - 1u));
-    const int base_node = inwin ? cell : 0;
-    for (int round = 0;; ++round) {
-      const bool mine = inwin && round_of_lane == round;
-#pragma unroll
-      for (int a = 0; a < 3; ++a)
-#pragma unroll
-        for (int bb = 0; bb < 3; ++bb) {
-          const float wab = wt[a][0] * wt[bb][1];
-          const float2 p0 = make_float2(mass, fmaf(adx[0][1], (float)bb, fmaf(adx[0][0], (float)a, q[0])));
-          const float2 p1 = make_float2(fmaf(adx[1][1], (float)bb, fmaf(adx[1][0], (float)a, q[1])),
-                                        fmaf(adx[2][1], (float)bb, fmaf(adx[2][0], (float)a, q[2])));
-          const float2 dz0 = make_float2(0.0f, adx[0][2]), dz1 = make_float2(adx[1][2], adx[2][2]);
-          float2 t0 = p0, t1 = p1;
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            // unconditional read and arithmetic, predicated store only
-            const float wgt = wab * wt[c][2];
-            const float2 w2 = make_float2(wgt, wgt);
-            float4 *nd = sm.tile + base_node + a * kP2GTileSX + bb * kP2GTileSY + c;
-            float4 g = *nd;
-            const float2 g01 = __ffma2_rn(w2, t0, make_float2(g.x, g.y));
-            const float2 g23 = __ffma2_rn(w2, t1, make_float2(g.z, g.w));
-            if (mine) *nd = make_float4(g01.x, g01.y, g23.x, g23.y);
-            __syncwarp();
-            if (c < 2) {
-              t0 = __fadd2_rn(t0, dz0);
-              t1 = __fadd2_rn(t1, dz1);
-            }
-          }
-        }
-      if (!__any_sync(0xffffffffu, inwin && round_of_lane > round)) break;
-    }
+    p2g_scatter_step<false>(P, w, sm.tile, o, anchored, act, bs, wt, mass, q, adx, lane);
     g0 = g1;
   }
-  if (anchored) p2g_tile_flush(P, w, sm.tile, o, lane);
+  if (anchored) p2g_tile_flush<false>(P, w, sm.tile, o, lane);
   set_status(w, bad);
   step_queue_done(w, kP2GQueue, kP2GDone, lane, nwarps);
 }
@@ -727,6 +761,9 @@ __global__ __launch_bounds__(256) void k_grid(const MpmParams P, const MpmParams
     const int64_t addr = (int64_t)blin * kBlockCells + l;
     const float4 g = w.grid_mom[addr];
     w.grid_mom[addr] = make_float4(0.f, 0.f, 0.f, 0.f);
+    // a fused substep flags the blocks it scatters into; the flags are used
+    // up once the grid-active list is built
+    if (l == 0) w.blk_flag[blin] = 0;
     int bx, by, bz;
     block_coords(P, blin, bx, by, bz);
     const MpmParams &S = scene_of_block<BATCH>(P, tab, bx, by, bz);
@@ -753,6 +790,7 @@ __global__ __launch_bounds__(kG2PThreads, 8) void k_g2p(const MpmParams P, const
   const int nitems = (int)min((int64_t)w.counters[2], w.items_cap);
   uint32_t bad = 0;
   float vmax = 0.0f;
+  float bmin[3] = {INFINITY, INFINITY, INFINITY}, bmax[3] = {-INFINITY, -INFINITY, -INFINITY};
   for (int it = blockIdx.x; it < nitems; it += gridDim.x) {
     const int2 item = w.items[it];
     const int k = item.x, start = item.y;
@@ -834,6 +872,11 @@ __global__ __launch_bounds__(kG2PThreads, 8) void k_g2p(const MpmParams P, const
         ld_v<Q>(st, cap, j, vv);
       }
       vmax = fmaxf(vmax, fmaxf(fabsf(vv[0]), fmaxf(fabsf(vv[1]), fabsf(vv[2]))));
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {  // fminf / fmaxf skip NaN positions
+        bmin[d] = fminf(bmin[d], x[d]);
+        bmax[d] = fmaxf(bmax[d], x[d]);
+      }
       if (BIN == kBinKeep) {  // next substep's build_pid, keeping the rank of a stayer
         const int old_key = cell_key(P, b);
         const int r_old = w.slot_rank[j];
@@ -858,6 +901,291 @@ __global__ __launch_bounds__(kG2PThreads, 8) void k_g2p(const MpmParams P, const
     for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
     if ((threadIdx.x & 31) == 0 && vmax > 0.0f) atomicMax((int *)maxv_out, __float_as_int(vmax));
   }
+  if (!BATCH) {  // bounding box of the advected particles (the host sizes the grid window with it)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        bmin[d] = fminf(bmin[d], __shfl_xor_sync(0xffffffffu, bmin[d], o));
+        bmax[d] = fmaxf(bmax[d], __shfl_xor_sync(0xffffffffu, bmax[d], o));
+      }
+      if ((threadIdx.x & 31) == 0 && bmin[d] <= bmax[d]) {
+        atomicMin(&w.counters[kBoxMin + d], float_key_i32(bmin[d]));
+        atomicMax(&w.counters[kBoxMax + d], float_key_i32(bmax[d]));
+      }
+    }
+  }
+}
+
+// --------------------------------------------- fused plain substeps ----
+//
+// A frame of the plain substep loop (engine/mpm_solver.py:789-797) can run
+// G2P of substep s-1 and P2G of substep s as one pass over the particles,
+// with the state updated in place in its storage order:
+//   sort       binning and the streaming P2G (k_p2g) into sorted order;
+//   fused      k_fused: per warp step of 32 slots, G2P of the previous
+//              substep at x (gather of the grid velocities through L1),
+//              advection, the constitutive update with the new C and the
+//              scatter at the new x into the warp's tile window; it flags the
+//              blocks that receive momentum, which make the grid-active list;
+//   close      k_g2p_stream: G2P of the last substep with the binning of the
+//              next sort.
+// The arithmetic is the plain substep's; only the order of the float32
+// summations differs.  The storage order drifts from the positions while
+// fused substeps run, so a frame re-sorts every few substeps.
+
+constexpr int kFusedQueue = 7, kFusedDone = 8;  // counters[]: step queue, warps done
+
+// Separable node addresses of the block-major grid around base b:
+// addr(b + (a, bb, c)) = ax[a] + ay[bb] + az[c].
+__device__ __forceinline__ void stencil_addresses(const MpmParams &P, const int (&b)[3], int (&ax)[3], int (&ay)[3],
+                                                  int (&az)[3]) {
+  const int SX = P.win_nb[1] * P.win_nb[2] * kBlockCells, SY = P.win_nb[2] * kBlockCells;
+#pragma unroll
+  for (int o = 0; o < 3; ++o) {
+    const int gx = b[0] + o, gy = b[1] + o, gz = b[2] + o;
+    ax[o] = (gx >> 2) * SX + (gx & 3) * 16;
+    ay[o] = (gy >> 2) * SY + (gy & 3) * 4;
+    az[o] = (gz >> 2) * kBlockCells + (gz & 3);
+  }
+}
+
+// G2P gather (:711-721) straight from the grid velocities: v and C.
+__device__ __forceinline__ void gather_vc(const MpmParams &P, const float4 *__restrict__ gv, const Base &b,
+                                          float (&nv)[3], float (&nC)[3][3]) {
+  float wt[3][3];
+  bspline_weights(b.fx, wt);
+  int ax[3], ay[3], az[3];
+  stencil_addresses(P, b.b, ax, ay, az);
+  float sa[3] = {0.f, 0.f, 0.f}, sb[3] = {0.f, 0.f, 0.f}, sc[3] = {0.f, 0.f, 0.f};
+  nv[0] = nv[1] = nv[2] = 0.0f;
+  const float wz0 = wt[0][2], wz1 = wt[1][2], wz2 = wt[2][2], wz2x2 = 2.0f * wt[2][2];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int bb = 0; bb < 3; ++bb) {
+      const int line = ax[a] + ay[bb];
+      const float4 g0 = __ldg(gv + line + az[0]), g1 = __ldg(gv + line + az[1]), g2 = __ldg(gv + line + az[2]);
+      const float2 T01 =
+          __ffma2_rn(f2(wz2, wz2), f2(g2.x, g2.y), __ffma2_rn(f2(wz1, wz1), f2(g1.x, g1.y), __fmul2_rn(f2(wz0, wz0), f2(g0.x, g0.y))));
+      const float T2 = fmaf(wz2, g2.z, fmaf(wz1, g1.z, wz0 * g0.z));
+      const float2 U01 = __ffma2_rn(f2(wz2x2, wz2x2), f2(g2.x, g2.y), __fmul2_rn(f2(wz1, wz1), f2(g1.x, g1.y)));
+      const float U2 = fmaf(wz2x2, g2.z, wz1 * g1.z);
+      const float W = wt[a][0] * wt[bb][1];
+      const float T[3] = {T01.x, T01.y, T2}, U[3] = {U01.x, U01.y, U2};
+#pragma unroll
+      for (int r = 0; r < 3; ++r) {
+        nv[r] = fmaf(W, T[r], nv[r]);
+        sc[r] = fmaf(W, U[r], sc[r]);
+        if (a > 0) sa[r] = fmaf((float)a * W, T[r], sa[r]);
+        if (bb > 0) sb[r] = fmaf((float)bb * W, T[r], sb[r]);
+      }
+    }
+  const float s4 = 4.0f * P.inv_dx;
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    nC[r][0] = s4 * fmaf(-nv[r], b.fx[0], sa[r]);
+    nC[r][1] = s4 * fmaf(-nv[r], b.fx[1], sb[r]);
+    nC[r][2] = s4 * fmaf(-nv[r], b.fx[2], sc[r]);
+  }
+}
+
+// Per-warp shared memory of the fused kernel: staged rows x (3) and F .. E
+// (9 + Jp + material + id + E), the tile, the mbarrier.
+constexpr int kFusedRowsF = 13;
+struct __align__(128) FusedWarpSmem {
+  float bx[3][32];  // 384 bytes: bf starts 128-byte aligned
+  float bf[kFusedRowsF][32];
+  float4 tile[kP2GTileN + 1];
+  unsigned long long bar;
+};
+static_assert(offsetof(FusedWarpSmem, bf) % 128 == 0 && sizeof(FusedWarpSmem) % 128 == 0,
+              "fused staging buffers must be 128-byte aligned");
+constexpr size_t kFusedSmem = sizeof(FusedWarpSmem) * kP2GWarps;
+
+// Stages step g of the fused kernel: rows x and F .. (NF rows from F on).
+template <int NF>
+__device__ __forceinline__ void fused_stage(FusedWarpSmem &sm, const CUtensorMap &map_x, const CUtensorMap &map_f,
+                                            int g, int lane) {
+  if (lane == 0) {
+    fence_proxy_async_smem();
+    mbar_arrive_expect_tx(&sm.bar, (3 + NF) * 128);
+    tma_load_2d(sm.bx[0], &map_x, g * 32, 0, &sm.bar);
+    tma_load_2d(sm.bf[0], &map_f, g * 32, PRows<false>::F, &sm.bar);
+  }
+}
+
+template <bool HAS_EP>
+__global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_fused(const MpmParams P, const Ws w,
+                                                                          const __grid_constant__ CUtensorMap map_x,
+                                                                          const __grid_constant__ CUtensorMap map_f,
+                                                                          float *__restrict__ st, int64_t cap,
+                                                                          int64_t n, float dt, float *maxv_out) {
+  using R = PRows<false>;
+  constexpr int NF = HAS_EP ? kFusedRowsF : kFusedRowsF - 2;  // F, Jp, material[, id, E]
+  extern __shared__ __align__(128) unsigned char fused_smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  FusedWarpSmem &sm = reinterpret_cast<FusedWarpSmem *>(fused_smem)[warp];
+  const int nsteps = (int)((n + 31) / 32);
+  const int nwarps = (int)gridDim.x * kP2GWarps;
+  uint32_t bad = 0;
+  float vmax = 0.0f;
+  for (int t = lane; t < kP2GTileN + 1; t += 32) sm.tile[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (lane == 0) {
+    mbar_init(&sm.bar, 1);
+    fence_mbar_init();
+  }
+  __syncwarp();
+  int q_next = 0, q_end = 0;
+  uint32_t parity = 0u;
+  int g0 = step_queue_next(w, kFusedQueue, lane, nsteps, nwarps, q_next, q_end);
+  if (g0 >= 0) fused_stage<NF>(sm, map_x, map_f, g0, lane);
+  bool anchored = false;
+  int o[3] = {0, 0, 0};
+  while (g0 >= 0) {
+    if (!mbar_wait(&sm.bar, parity)) {
+      bad |= MPM_STATUS_TIMEOUT;
+      anchored = false;
+      break;
+    }
+    parity ^= 1u;
+    float x[3], F[3][3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) x[d] = sm.bx[d][lane];
+#pragma unroll
+    for (int a = 0; a < 9; ++a) F[a / 3][a % 3] = sm.bf[a][lane];
+    float Jp = sm.bf[9][lane];
+    const int matword = __float_as_int(sm.bf[10][lane]);
+    const float Ep = HAS_EP ? sm.bf[12][lane] : 0.0f;
+    __syncwarp();
+    const int g1 = step_queue_next(w, kFusedQueue, lane, nsteps, nwarps, q_next, q_end);
+    if (g1 >= 0) fused_stage<NF>(sm, map_x, map_f, g1, lane);
+    const int64_t i = (int64_t)g0 * 32 + lane;
+    const bool act = i < n;
+    const int mat = matword & 0xFF;
+    float v[3] = {0.f, 0.f, 0.f}, C[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+    uint32_t bad_b = 0;
+    if (act) {
+      // G2P of the previous substep, :694-724
+      const Base b0 = particle_base(P, x[0], x[1], x[2], bad_b);
+      if (mat != 4) {
+        gather_vc(P, w.grid_vel, b0, v, C);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          st[(R::V + d) * cap + i] = v[d];
+          x[d] = x[d] + dt * v[d];
+          st[(R::X + d) * cap + i] = x[d];
+        }
+#pragma unroll
+        for (int a = 0; a < 9; ++a) st[(R::C + a) * cap + i] = C[a / 3][a % 3];
+      } else {  // stationary: v, C and x stay
+#pragma unroll
+        for (int d = 0; d < 3; ++d) v[d] = st[(R::V + d) * cap + i];
+#pragma unroll
+        for (int a = 0; a < 9; ++a) C[a / 3][a % 3] = st[(R::C + a) * cap + i];
+      }
+      vmax = fmaxf(vmax, fmaxf(fabsf(v[0]), fmaxf(fabsf(v[1]), fabsf(v[2]))));
+    }
+    // P2G of this substep at the advected x, :487-584
+    Base bs = particle_base(P, x[0], x[1], x[2], bad_b);
+    if (act) bad |= bad_b;
+    float mass = 0.f, q[3] = {0.f, 0.f, 0.f}, adx[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+    float wt[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+    if (act) {
+      const P2GOut out = constitutive(P, dt, mat, Ep, F, Jp, C);
+#pragma unroll
+      for (int a = 0; a < 9; ++a) st[(R::F + a) * cap + i] = F[a / 3][a % 3];
+      st[R::Jp * cap + i] = Jp;
+      bspline_weights(bs.fx, wt);
+      mass = out.mass;
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+        q[d] = out.mass * v[d] -
+               P.dx * (out.affine[d][0] * bs.fx[0] + out.affine[d][1] * bs.fx[1] + out.affine[d][2] * bs.fx[2]);
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) adx[r][c] = out.affine[r][c] * P.dx;
+    }
+    p2g_scatter_step<true>(P, w, sm.tile, o, anchored, act, bs, wt, mass, q, adx, lane);
+    g0 = g1;
+  }
+  if (anchored) p2g_tile_flush<true>(P, w, sm.tile, o, lane);
+  set_status(w, bad);
+  if (maxv_out) {
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, d));
+    if (lane == 0 && vmax > 0.0f) atomicMax((int *)maxv_out, __float_as_int(vmax));
+  }
+  step_queue_done(w, kFusedQueue, kFusedDone, lane, nwarps);
+}
+
+// G2P of the last substep of a fused run, in the storage order, with the
+// plain binning for the next sort (in-cell ranks from arrival order: the
+// storage order no longer matches the last sort's ranks), the max |v| and
+// the particles' bounding box.
+__global__ __launch_bounds__(128, 5) void k_g2p_stream(const MpmParams P, const Ws w, float *__restrict__ st,
+                                                      int64_t cap, int64_t n, float dt, float *maxv_out) {
+  using R = PRows<false>;
+  const int lane = threadIdx.x & 31;
+  const int nsteps = (int)((n + 31) / 32);
+  const int nwarps = (int)gridDim.x * (blockDim.x >> 5);
+  uint32_t bad = 0;
+  float vmax = 0.0f;
+  float bmin[3] = {INFINITY, INFINITY, INFINITY}, bmax[3] = {-INFINITY, -INFINITY, -INFINITY};
+  int q_next = 0, q_end = 0;
+  for (int g = step_queue_next(w, kFusedQueue, lane, nsteps, nwarps, q_next, q_end); g >= 0;
+       g = step_queue_next(w, kFusedQueue, lane, nsteps, nwarps, q_next, q_end)) {
+    const int64_t j = (int64_t)g * 32 + lane;
+    if (j >= n) continue;
+    float x[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) x[d] = st[(R::X + d) * cap + j];
+    const int matword = __float_as_int(st[R::Mat * cap + j]);
+    const Base b = particle_base(P, x[0], x[1], x[2], bad);
+    float vv[3];
+    if ((matword & 0xFF) != 4) {
+      float nC[3][3];
+      gather_vc(P, w.grid_vel, b, vv, nC);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        st[(R::V + d) * cap + j] = vv[d];
+        x[d] = x[d] + dt * vv[d];
+        st[(R::X + d) * cap + j] = x[d];
+      }
+#pragma unroll
+      for (int a = 0; a < 9; ++a) st[(R::C + a) * cap + j] = nC[a / 3][a % 3];
+    } else {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) vv[d] = st[(R::V + d) * cap + j];
+    }
+    vmax = fmaxf(vmax, fmaxf(fabsf(vv[0]), fmaxf(fabsf(vv[1]), fabsf(vv[2]))));
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      bmin[d] = fminf(bmin[d], x[d]);
+      bmax[d] = fmaxf(bmax[d], x[d]);
+    }
+    bin_one<false>(P, nullptr, w, j, x[0], x[1], x[2], matword, bad);
+  }
+  set_status(w, bad);
+  if (maxv_out) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+    if (lane == 0 && vmax > 0.0f) atomicMax((int *)maxv_out, __float_as_int(vmax));
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      bmin[d] = fminf(bmin[d], __shfl_xor_sync(0xffffffffu, bmin[d], o));
+      bmax[d] = fmaxf(bmax[d], __shfl_xor_sync(0xffffffffu, bmax[d], o));
+    }
+    if (lane == 0 && bmin[d] <= bmax[d]) {
+      atomicMin(&w.counters[kBoxMin + d], float_key_i32(bmin[d]));
+      atomicMax(&w.counters[kBoxMax + d], float_key_i32(bmax[d]));
+    }
+  }
+  step_queue_done(w, kFusedQueue, kFusedDone, lane, nwarps);
 }
 
 // -------------------------------------------------------------- G2P2G ----
@@ -1135,13 +1463,14 @@ static EncodeTiledFn encode_tiled() {
 }
 
 // Tensor map of the first `rows` rows of a state buffer: a 2-D float32
-// tensor of cap x rows elements (row stride cap), boxes of 32 slots x rows.
-static bool rows_tensor_map(CUtensorMap *map, const float *state, int64_t cap, int rows) {
+// tensor of cap x rows elements (row stride cap), boxes of 32 slots x
+// box_rows rows (box_rows = rows when 0).
+static bool rows_tensor_map(CUtensorMap *map, const float *state, int64_t cap, int rows, int box_rows = 0) {
   const EncodeTiledFn fn = encode_tiled();
   if (!fn) return false;
   const cuuint64_t dims[2] = {(cuuint64_t)cap, (cuuint64_t)rows};
   const cuuint64_t strides[1] = {(cuuint64_t)cap * sizeof(float)};
-  const cuuint32_t box[2] = {32u, (cuuint32_t)rows};
+  const cuuint32_t box[2] = {32u, (cuuint32_t)(box_rows > 0 ? box_rows : rows)};
   const cuuint32_t elem[2] = {1u, 1u};
   return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(state), dims, strides, box, elem,
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -1178,6 +1507,7 @@ struct DevInfo {
   int p2g_ctas = 0, p2g_ep_ctas = 0, g2p_ctas = 0, g2p2g_ctas = 0;
   int p2g_b_ctas = 0, p2g_ep_b_ctas = 0, g2p_b_ctas = 0;
   int p2g_q_ctas = 0, p2g_ep_q_ctas = 0, g2p_q_ctas = 0, g2p2g_q_ctas = 0;  // packed storage
+  int fused_ctas = 0, fused_ep_ctas = 0, g2ps_ctas = 0;  // fused plain substeps
 };
 
 static DevInfo g_dev[64];
@@ -1215,6 +1545,17 @@ static const DevInfo *dev_info() {
     d.p2g_b_ctas = sms * (a2 > 0 ? a2 : 1);
     d.p2g_ep_b_ctas = sms * (b2 > 0 ? b2 : 1);
     d.g2p_b_ctas = sms * (c2 > 0 ? c2 : 1);
+    {
+      int fa = 0, fb = 0, gs = 0;
+      cudaFuncSetAttribute(k_fused<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFusedSmem);
+      cudaFuncSetAttribute(k_fused<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFusedSmem);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fa, k_fused<false>, kP2GThreads, kFusedSmem);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fb, k_fused<true>, kP2GThreads, kFusedSmem);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&gs, k_g2p_stream, 128, 0);
+      d.fused_ctas = sms * (fa > 0 ? fa : 1);
+      d.fused_ep_ctas = sms * (fb > 0 ? fb : 1);
+      d.g2ps_ctas = sms * (gs > 0 ? gs : 1);
+    }
     d.sms = sms;
   }
   return &d;
@@ -1424,6 +1765,25 @@ int mpm_substep(const MpmParams *p, void *ws, int64_t cap, int64_t n, const floa
   return mpm_g2p(p, ws, cap, n, nxt, dt, maxv_out, stream);
 }
 
+// One fused substep on `st` in place: G2P of the previous substep and P2G
+// of this one (k_fused), the grid-active list from the flagged blocks, the
+// grid update.
+static int fused_substep(const DevInfo *di, cudaStream_t s, const MpmParams &p, const Ws &w, float *st, int64_t cap,
+                         int64_t n, float dt, float *maxv) {
+  CUtensorMap mx, mf;
+  const int nf = p.has_Ep ? kFusedRowsF : kFusedRowsF - 2;
+  if (!rows_tensor_map(&mx, st, cap, MPM_NROWS, 3) || !rows_tensor_map(&mf, st, cap, MPM_NROWS, nf))
+    return MPM_E_CUDA;
+  if (p.has_Ep)
+    k_fused<true><<<di->fused_ep_ctas, kP2GThreads, kFusedSmem, s>>>(p, w, mx, mf, st, cap, n, dt, maxv);
+  else
+    k_fused<false><<<di->fused_ctas, kP2GThreads, kFusedSmem, s>>>(p, w, mx, mf, st, cap, n, dt, maxv);
+  k_flags_count<<<w.nflagtiles, 256, 0, s>>>(p, w);
+  k_flags_write<<<w.nflagtiles, 256, 0, s>>>(p, w);
+  k_grid<false><<<di->sms * 8, 256, 0, s>>>(p, nullptr, w, dt);
+  return last_error();
+}
+
 static bool batch_ok(const MpmParams *p) {
   if (!params_ok(p) || p->n_scenes < 1 || p->quant) return false;
   int64_t slots = 1;
@@ -1499,6 +1859,41 @@ int mpm_substep_noalloc(const MpmParams *p, int64_t cap, int64_t n, const float 
     // the next call bins from scratch, so G2P skips the binning
     k_g2p<false, false, kBinNone><<<di->g2p_ctas, kG2PThreads, 0, s>>>(*p, nullptr, w, nxt, cap, dt, maxv_out);
   }
+  return last_error();
+}
+
+int mpm_frame(const MpmParams *p, void *ws, int64_t cap, int64_t n, float *a, float *b, float dt, int32_t count,
+              int32_t resort, float *maxv, int32_t *in_b, void *stream) {
+  if (!params_ok(p) || p->quant || p->n_scenes > 0 || !ws || !a || !b || !maxv || !in_b || n < 0 || n > cap ||
+      count < 1 || resort < 1 || !p2g_rows_ok(a, cap) || !p2g_rows_ok(b, cap))
+    return MPM_E_INVALID;
+  const DevInfo *di = dev_info();
+  if (!di) return MPM_E_CUDA;
+  Ws w;
+  ws_layout(*p, cap, (char *)ws, &w);
+  cudaStream_t s = (cudaStream_t)stream;
+  float *cur = a, *oth = b;
+  int rc = MPM_OK;
+  for (int k = 0; k < count; ++k) {
+    if (k % resort == 0) {
+      // close the previous substep with the binning of this sort, then sort
+      if (k > 0 && n > 0)
+        k_g2p_stream<<<di->g2ps_ctas, 128, 0, s>>>(*p, w, cur, cap, n, dt, maxv + k - 1);
+      rc = mpm_bin_finalize(p, ws, cap, n, stream);
+      if (rc) return rc;
+      rc = launch_p2g_single(di, s, *p, w, cur, oth, cap, n, dt);
+      if (rc) return rc;
+      k_grid<false><<<di->sms * 8, 256, 0, s>>>(*p, nullptr, w, dt);
+      float *t = cur;
+      cur = oth;
+      oth = t;
+    } else if (n > 0) {
+      rc = fused_substep(di, s, *p, w, cur, cap, n, dt, maxv + k - 1);
+      if (rc) return rc;
+    }
+  }
+  if (n > 0) k_g2p_stream<<<di->g2ps_ctas, 128, 0, s>>>(*p, w, cur, cap, n, dt, maxv + count - 1);
+  *in_b = cur == b;
   return last_error();
 }
 

@@ -168,6 +168,9 @@ class MPMSolver:
         self.writers = []
 
         self.per_particle_E = bool(per_particle_E)
+        # fused frames re-sort the particles by grid block every this many
+        # substeps (the storage order drifts from the positions in between)
+        self.resort_every = 8
         self.chunk = int(chunk) if chunk else self.DEFAULT_CHUNK
         self.use_cuda_graph = use_cuda_graph
         self.autotune = bool(autotune)
@@ -204,6 +207,10 @@ class MPMSolver:
         self._mesh_seed = 0
         self._seed_lo = None  # bounding box (in nodes) of all seeded regions
         self._seed_hi = None
+        # bounding box (lo, hi) of the particle positions, known without a
+        # device reduction after a frame's readback; None when unknown
+        self._host_box = None
+        self._readback = None  # page-locked buffers of the end-of-frame readback
         self._set_window(*self._box_window())
 
     # ---------------------------------------------------------- params ---
@@ -492,6 +499,9 @@ class MPMSolver:
         if self.quant and any(not (-2.0 <= float(c) < 2.0) for c in list(lo) + list(hi)):
             raise ValueError("quant=True stores positions as fixed point in [-2, 2)")
         self._cover(lo, hi)
+        if self._host_box is not None:  # new particles inside [lo, hi]: the union bounds all
+            blo, bhi = self._host_box
+            self._host_box = ([min(a, float(b)) for a, b in zip(blo, lo)], [max(a, float(b)) for a, b in zip(bhi, hi)])
 
     @staticmethod
     def _finite_bounds(x: torch.Tensor):
@@ -613,21 +623,53 @@ class MPMSolver:
         self.n_particles = 0
         self._binned = 0
         self._ws = None
+        self._host_box = None
 
     # ------------------------------------------------------------- step ---
 
     def _check_window_covers_particles(self, frame_dt: float):
-        """Grow the grid window if particles got close to its edge."""
+        """Grow the grid window if particles got close to its edge.  The
+        particles' bounding box comes from the last frame's readback when it
+        is known (G2P reduces it on the device), else from a reduction here."""
         if self.n_particles == 0:
             return
-        mn, mx = self._finite_bounds(self._positions_f32())
+        if self._host_box is not None:
+            mn, mx = self._host_box
+        else:
+            mn, mx = self._finite_bounds(self._positions_f32())
         reach = (max(self.all_time_max_velocity, 1.0) * frame_dt * 2.0)
         self._cover([a - reach for a in mn], [b + reach for b in mx])
         if self._ws is None:
             self._rebin()
 
+    def _frame_readback(self, count: int):
+        """The one synchronisation of a frame: copies the per-substep max |v|
+        and the workspace counters (status word, the particles' bounding box
+        after the last substep) into page-locked buffers, raises on a device
+        status, and returns the max |v| per substep."""
+        if self._readback is None or self._readback[0].numel() < count:
+            self._readback = (torch.empty(max(count, 64), dtype=torch.float32, pin_memory=True),
+                              torch.empty(32, dtype=torch.int32, pin_memory=True))
+        hv, hc = self._readback
+        hv[:count].copy_(self._maxv[:count], non_blocking=True)
+        hc.copy_(self._ws[:128].view(torch.int32), non_blocking=True)
+        torch.cuda.current_stream(self.device).synchronize()
+        maxv = hv[:count].numpy().copy()
+        c = hc.numpy()
+        self._raise_status(int(c[3]))
+        keys = c[16:22].astype(np.int32)
+        bits = np.where(keys >= 0, keys, keys ^ np.int32(0x7FFFFFFF)).astype(np.int32)
+        box = bits.view(np.float32).astype(np.float64)
+        if np.all(np.isfinite(box)) and np.all(box[:3] <= box[3:]):
+            self._host_box = (box[:3].tolist(), box[3:].tolist())
+        else:
+            self._host_box = None
+        return maxv
+
     def _check_status(self):
-        st = int(self._status.item())
+        self._raise_status(int(self._status.item()))
+
+    def _raise_status(self, st: int):
         if st:
             self._status.zero_()
             msgs = []
@@ -675,6 +717,7 @@ class MPMSolver:
     def substep(self, dt: float):
         """One substep (engine/mpm_solver.py:789-797) with time step dt."""
         self._prepare(dt)
+        self._host_box = None  # positions move without a readback
         if self.n_particles == 0:
             self.t += dt
             return
@@ -696,36 +739,62 @@ class MPMSolver:
             frame_time_left -= dt
         return count, dt
 
+    @property
+    def _fuses_frames(self) -> bool:
+        """Frames of the plain substep run as fused substeps (mpm_frame):
+        float32 storage and the reference's plain loop (not use_g2p2g)."""
+        return not self.quant and not self.use_g2p2g
+
+    def _launch_frame(self, count: int, dt: float):
+        """All substeps of a frame: the plain loop fused (G2P of one substep
+        with P2G of the next), re-sorted every `resort_every` substeps."""
+        p = self.params
+        in_b = ctypes.c_int32(0)
+        _lib.check(
+            self._lib.mpm_frame(ctypes.byref(p), _ptr(self._ws), self._cap, self.n_particles,
+                                _ptr(self._state[self._cur]), _ptr(self._state[1 - self._cur]), float(dt), int(count),
+                                int(self.resort_every), _ptr(self._maxv), ctypes.byref(in_b), self.stream),
+            "mpm_frame")
+        self._cur = (self._cur + int(in_b.value)) % 2
+
+    def _frame_swaps(self, count: int) -> int:
+        """Buffer swaps of a fused frame: one per sort."""
+        return (count + self.resort_every - 1) // self.resort_every
+
+    def _launch_substeps(self, count: int, dt: float):
+        self._maxv[:count].zero_()
+        if self._fuses_frames:
+            self._launch_frame(count, dt)
+        else:
+            for s in range(count):
+                self._launch_substep(dt, s)
+
     def _run_frame(self, count: int, dt: float):
         """Run `count` substeps, through a CUDA graph when enabled."""
         if count > self._maxv.numel():
             self._maxv = torch.zeros(count, dtype=torch.float32, device=self.device)
-        key = (count, float(dt), self._cur, self.n_particles, self._params_version, _ptr(self._ws))
+        key = (count, float(dt), self._cur, self.n_particles, self._params_version, _ptr(self._ws),
+               self.resort_every)
         if self.use_g2p2g:  # the first substep's launch depends on the mode's state
             key += (bool(self._g2p2g_listed), self._last_final if self._g2p2g_grid_valid else 0)
         if not self.use_cuda_graph:
-            self._maxv[:count].zero_()
-            for s in range(count):
-                self._launch_substep(dt, s)
+            self._launch_substeps(count, dt)
             return
         g = self._graphs.get(key)
         if g is None and key in self._graph_seen:
             start_cur = self._cur
             g = torch.cuda.CUDAGraph()
             with torch.cuda.graph(g):
-                self._maxv[:count].zero_()
-                for s in range(count):
-                    self._launch_substep(dt, s)
+                self._launch_substeps(count, dt)
             self._cur = start_cur  # capture does not execute
             self._graphs[key] = g
         if g is not None:
             g.replay()
-            self._cur = (self._cur + count) % 2
+            swaps = self._frame_swaps(count) if self._fuses_frames else count
+            self._cur = (self._cur + swaps) % 2
             return
         self._graph_seen.add(key)
-        self._maxv[:count].zero_()
-        for s in range(count):
-            self._launch_substep(dt, s)
+        self._launch_substeps(count, dt)
 
     def step(self, frame_dt, print_stat=False, smry_writer=None):
         """engine/mpm_solver.py:748-821."""
@@ -740,6 +809,7 @@ class MPMSolver:
             tune_chunk(self)
             self._tuned = True
         if self.use_adaptive_dt:
+            self._host_box = None
             dts = self._adaptive_frame(frame_dt, dt)
             count = len(dts)
             maxv = self._maxv[:count].cpu().numpy() if self.n_particles > 0 else np.zeros(count, np.float32)
@@ -747,8 +817,12 @@ class MPMSolver:
                 self._check_status()
         elif self.n_particles > 0:
             self._run_frame(count, dt)
-            maxv = self._maxv[:count].cpu().numpy()
-            self._check_status()
+            if self.use_g2p2g:  # the fused kernel does not reduce the bounding box
+                maxv = self._maxv[:count].cpu().numpy()
+                self._check_status()
+                self._host_box = None
+            else:
+                maxv = self._frame_readback(count)
             dts = [dt] * count
         else:
             maxv = np.zeros(count, dtype=np.float32)

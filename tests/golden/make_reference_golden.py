@@ -146,8 +146,30 @@ def case_no_plasticity(rng):
     return dict(res=(24, 24, 24), state=s, postprocess=pp, kw=dict(support_plasticity=False))
 
 
+def case_degenerate(rng):
+    """Deformation gradients that stress the SVD convention, for every
+    material that takes the SVD: inverted (det F < 0), rank-deficient,
+    repeated and nearly repeated singular values, strong stretch and strong
+    compression, each rotated at random."""
+    s = evolved_state(rng, [(0.3, 0.5, 0.3), (0.6, 0.5, 0.35), (0.35, 0.5, 0.65), (0.65, 0.5, 0.65)], 0.06, 240,
+                      [MAT_ELASTIC, MAT_SNOW, MAT_SAND, MAT_STATIONARY], v_amp=0.3)
+    kinds = [np.diag([1.0, 1.0, -1.0]), np.diag([1.0, 0.8, 0.0]), np.eye(3) * 1.001, np.diag([1.02, 1.02, 0.99]),
+             np.diag([1.0, 1.0, 1.0 + 1e-6]), np.diag([2.5, 0.4, 1.0]), np.diag([0.5, 0.6, 0.7]),
+             np.diag([1.03, -0.97, 1.0])]
+    n = len(s["x"])
+    F = np.empty((n, 3, 3))
+    for p in range(n):
+        R1, R2 = _rot(rng), _rot(rng)
+        F[p] = R1 @ kinds[p % len(kinds)] @ R2.T
+    s["F"] = F.astype(np.float32)
+    s["C"] = (0.3 * s["C"]).astype(np.float32)
+    # one substep only: a rank-deficient snow particle ends with Jp = 0 (its
+    # hardening becomes e^10), which makes a longer trajectory meaningless
+    return dict(res=(24, 24, 24), state=s, postprocess=[], kw={}, no_trajectory=True)
+
+
 CASES = {"mixed_24": case_mixed, "walls_24": case_walls, "unbounded_24": case_unbounded,
-         "no_plasticity_24": case_no_plasticity}
+         "no_plasticity_24": case_no_plasticity, "degenerate_24": case_degenerate}
 
 
 # ------------------------------------------------------------ running ----
@@ -226,6 +248,8 @@ def run_case(MPMSolver, name, fn, traj_substeps=6):
             out = one_substep(s, dt)
         print(f"  {name} {prec}: one substep {time.time() - t0:.1f} s, {len(out['grid_nodes'])} nodes")
         res.update({f"{prec}_{k}": v for k, v in out.items()})
+    if case.get("no_trajectory"):
+        return res
     # trajectory through MPMSolver.step itself, float64
     ti.set_precision("f64")
     s = make_solver(MPMSolver, case)

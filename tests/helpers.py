@@ -103,7 +103,7 @@ def run_phases(solver, dt):
 
 # ------------------------------------------- reference-run fixtures ----
 
-REF_CASES = ["mixed_24", "walls_24", "unbounded_24", "no_plasticity_24"]
+REF_CASES = ["mixed_24", "walls_24", "unbounded_24", "no_plasticity_24", "degenerate_24"]
 
 
 def ref_fixture(name):
@@ -148,3 +148,30 @@ def ref_particles(g, dtype=np.float64):
     return O.Particles(np.ascontiguousarray(g["in_x"], dtype), np.ascontiguousarray(g["in_v"], dtype),
                        np.ascontiguousarray(C, dtype), np.ascontiguousarray(g["in_F"], dtype),
                        np.ascontiguousarray(Jp, dtype), np.ascontiguousarray(g["in_material"], np.int32))
+
+
+# -------------------------------------------------- tolerance table ----
+# Relative L-inf bounds of one GPU substep against float64 (the oracle or
+# the reference's own run).  Spec bounds: grid m / mv 1e-5, particle
+# x / F 1e-6 (Jp on F's scale).  Calibrated (the reference's own float32 run
+# is farther than the benchmark spec's 1e-6 from its float64 run, see
+# tests/test_gpu_reference_golden.py): v 1e-5, grid v 1e-5, C 2e-5.
+BOUND = {"grid_m": 1e-5, "grid_mv": 1e-5, "grid_v": 1e-5, "x": 1e-6, "F": 1e-6, "Jp": 1e-6, "v": 1e-5, "C": 2e-5}
+
+
+def assert_bounds(label, errs, bounds=None, f32_calibrated=False):
+    """errs: field -> (gpu error, float32-oracle error).  Prints every field
+    and asserts the GPU error against the bound table.  With
+    f32_calibrated (states where a float32 evaluation of the reference
+    algorithm is itself farther from float64 than the table, measured by the
+    float32 oracle on the same state: evolved and multi-substep states), a
+    field's bound is raised to 4x the float32 oracle's own error where that
+    is larger; such fields print with '*'."""
+    bounds = dict(BOUND if bounds is None else bounds)
+    eff, mark = {}, {}
+    for k, (g, f) in errs.items():
+        eff[k] = max(bounds[k], 4 * f) if f32_calibrated else bounds[k]
+        mark[k] = "*" if eff[k] > bounds[k] else ""
+    print(f"\n{label}: " + " ".join(f"{k}={g:.2e}(f32 {f:.1e})/{eff[k]:.1e}{mark[k]}" for k, (g, f) in errs.items()))
+    bad = {k: g for k, (g, f) in errs.items() if not g <= eff[k]}
+    assert not bad, f"{label}: above the bound: {bad}"

@@ -13,11 +13,11 @@ import numpy as np
 import pytest
 import torch
 
-from helpers import oracle_config
+from helpers import assert_bounds, oracle_config
 from oracle import oracle as O
 from taichi_elements_gb300 import scenes
-from test_gpu_g2p2g import TOL as TOL_FUSED, errors as fused_errors
-from test_gpu_parity import TOL, _one_substep_errors
+from test_gpu_g2p2g import errors as fused_errors
+from test_gpu_parity import _one_substep_errors
 
 pytestmark = pytest.mark.gpu
 
@@ -43,8 +43,7 @@ def test_one_substep_parity_sheared(plasticity):
     torch.cuda.synchronize()
     jp0 = s.full_state()['Jp'].cpu().numpy()
     errs = _one_substep_errors(s, sc.default_dt)
-    for k, (g, f32) in errs.items():
-        assert g <= max(TOL[k], 4 * f32), f"{k}: gpu {g:.3g} vs f32-oracle {f32:.3g}"
+    assert_bounds(f"sheared four materials, plasticity {plasticity}", errs, f32_calibrated=True)
     if not plasticity:
         np.testing.assert_array_equal(s.full_state()['Jp'].cpu().numpy(), jp0)
 
@@ -83,5 +82,5 @@ def test_g2p2g_without_plasticity_matches_oracle():
         s.substep(dt)
         R64.step(dt)
         R32.step(dt)
-    for k, (g, f32) in fused_errors(s, R64, R32, win).items():
-        assert g <= max(TOL_FUSED[k], 4 * f32), f"{k}: gpu {g:.3g} vs f32-oracle {f32:.3g}"
+    assert_bounds("sheared four materials, fused, no plasticity, 8 substeps", fused_errors(s, R64, R32, win),
+                  f32_calibrated=True)

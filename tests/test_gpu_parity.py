@@ -13,8 +13,8 @@ import numpy as np
 import pytest
 import torch
 
-from helpers import (block_coords, lib_call, oracle_config, particles_from_solver, rel_inf, run_phases,
-                     window_lookup)
+from helpers import (assert_bounds, block_coords, lib_call, oracle_config, particles_from_solver, rel_inf,
+                     run_phases, window_lookup)
 from oracle import oracle as O
 from taichi_elements_gb300 import scenes
 from taichi_elements_gb300.mpm_solver import MPMSolver, MPMError
@@ -64,13 +64,13 @@ def _evolve(sc, n_sub, **kw):
     return s
 
 
-def _one_substep_errors(s, dt):
+def _one_substep_errors(s, dt, nthreads=1):
     cfg = oracle_config(s)
     P64 = particles_from_solver(s, np.float64)
     P32 = particles_from_solver(s, np.float32)
     win = O.Window.covering(P64.x, cfg.inv_dx)
-    _, gm64, gmv64, gv64 = O.substep(cfg, P64, dt, win)
-    _, gm32, gmv32, gv32 = O.substep(cfg, P32, dt, win)
+    _, gm64, gmv64, gv64 = O.substep(cfg, P64, dt, win, nthreads)
+    _, gm32, gmv32, gv32 = O.substep(cfg, P32, dt, win, nthreads)
     views, out = run_phases(s, dt)
     Pg = particles_from_solver(s, np.float64)
     coords, mom = out['mom']
@@ -98,16 +98,12 @@ def _one_substep_errors(s, dt):
     return errs
 
 
-TOL = {'grid_m': 1e-5, 'grid_mv': 1e-5, 'grid_v': 1e-5, 'x': 1e-6, 'v': 1e-5, 'F': 1e-6, 'Jp': 1e-6, 'C': 1e-5}
-
-
 @pytest.mark.parametrize("scene_fn,n_pre", [(scenes.smoke_scene, 40), (lambda: scenes.four_materials_128(per_cube=20000), 30)])
 def test_one_substep_parity(scene_fn, n_pre):
     sc = scene_fn()
     s = _evolve(sc, n_pre)
     errs = _one_substep_errors(s, sc.default_dt)
-    for k, (g, f32) in errs.items():
-        assert g <= max(TOL[k], 4 * f32), f"{k}: gpu {g:.3g} vs f32-oracle {f32:.3g}"
+    assert_bounds(sc.name, errs, f32_calibrated=True)
 
 
 def _dense_swirl_scene():
@@ -133,8 +129,7 @@ def test_one_substep_parity_dense_cells():
     s = _evolve(sc, 10)
     s._check_status()
     errs = _one_substep_errors(s, sc.default_dt)
-    for k, (g, f32) in errs.items():
-        assert g <= max(TOL[k], 4 * f32), f"{k}: gpu {g:.3g} vs f32-oracle {f32:.3g}"
+    assert_bounds(sc.name, errs, f32_calibrated=True)
     s.substep(sc.default_dt)
     s._check_status()
 

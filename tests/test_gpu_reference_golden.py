@@ -65,6 +65,26 @@ def make_solver(g, **extra):
     return s
 
 
+# States whose float32 evaluation is ill-conditioned even in the reference:
+# degenerate_24 (inverted, rank-deficient, repeated-singular-value F for every
+# material) exists to pin the SVD sign convention, where a wrong convention
+# would make errors of order 1.  The reference's own float32 run is up to
+# 6e-4 from its float64 run there, so the bound is 8x that distance.
+NOISY = {"degenerate_24"}
+
+
+def _reference_f32_noise(g):
+    vs = max(np.abs(g["f64_out_v"]).max(), 1e-3)
+    out = {"grid_m": rel_inf(g["f32_grid_m"], g["f64_grid_m"]), "grid_mv": rel_inf(g["f32_grid_mv"], g["f64_grid_mv"]),
+           "grid_v": rel_inf(g["f32_grid_v"], g["f64_grid_v"]),
+           "x": rel_inf(g["f32_out_x"], g["f64_out_x"], 1.0), "v": rel_inf(g["f32_out_v"], g["f64_out_v"], vs),
+           "F": rel_inf(g["f32_out_F"], g["f64_out_F"], max(1.0, np.abs(g["f64_out_F"]).max())),
+           "C": rel_inf(g["f32_out_C"], g["f64_out_C"])}
+    out["Jp"] = rel_inf(g["f32_out_Jp"], g["f64_out_Jp"], max(1.0, np.abs(g["f64_out_Jp"]).max())) \
+        if "f32_out_Jp" in g else 0.0
+    return out
+
+
 def _lookup(coords, ref_nodes, ref_vals):
     """Reference values at the engine's node coordinates (0 where the
     reference has no active block)."""
@@ -107,15 +127,21 @@ def test_gpu_substep_matches_reference_run(name):
            "C": rel_inf(st["C"].cpu().numpy(), g["f64_out_C"])}
     if "f64_out_Jp" in g:
         err["Jp"] = rel_inf(st["Jp"].cpu().numpy(), g["f64_out_Jp"], max(1.0, np.abs(g["f64_out_Jp"]).max()))
-    print(f"\n{name}: " + " ".join(f"{k}={v:.2e}/{BOUND[k]:.0e}" for k, v in err.items()))
+    bound = dict(BOUND)
+    if name in NOISY:  # ill-conditioned states: 8x the reference float32 run's own error
+        noise = _reference_f32_noise(g)
+        bound = {k: max(BOUND[k], 8 * noise[k]) for k in BOUND}
+    print(f"\n{name}: " + " ".join(f"{k}={v:.2e}/{bound[k]:.1e}" for k, v in err.items()))
     for k, e in err.items():
-        assert e <= BOUND[k], f"{k}: {e:.3g} > {BOUND[k]:.0e}"
+        assert e <= bound[k], f"{k}: {e:.3g} > {bound[k]:.1e}"
     assert int(s._status.item()) == 0
 
 
 @pytest.mark.parametrize("name", REF_CASES)
 def test_gpu_step_trajectory_matches_reference_step(name):
     g = ref_fixture(name)
+    if "traj_x" not in g:
+        pytest.skip("no trajectory for this state")
     s = make_solver(g)
     s.step(float(g["traj_frame_dt"]))
     assert s.total_substeps == int(g["traj_substeps"])
@@ -141,3 +167,16 @@ def test_gpu_fused_mode_matches_reference_g2p2g():
         eJ = rel_inf(st["Jp"].cpu().numpy(), g[f"sub{k}_Jp"], 1.0)
         print(f"\ng2p2g substep {k}: x={ex:.2e} v={ev:.2e} F={eF:.2e} Jp={eJ:.2e}")
         assert ex <= BOUND["x"] and ev <= BOUND["v"] and eF <= 2e-6 and eJ <= 2e-6
+
+
+@pytest.mark.parametrize("name", REF_CASES)
+def test_gpu_max_velocity_matches_reference(name):
+    """compute_max_velocity (engine/mpm_solver.py:726-735): the largest
+    |v_i| over the particles after G2P, as the substep records it."""
+    g = ref_fixture(name)
+    s = make_solver(g)
+    s.substep(float(g["dt"]))
+    got = float(s._maxv[0].item())
+    ref = float(g["f64_maxv"])
+    print(f"\n{name}: max |v| {got:.7g} (reference {ref:.7g})")
+    assert abs(got - ref) <= (8 * max(_reference_f32_noise(g)["v"], 1e-6)) * ref

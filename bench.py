@@ -1,18 +1,22 @@
 #!/usr/bin/env python
 """Benchmark of the GB300 MLS-MPM engine: particle-substeps/s.
 
-A "step" is one MLS-MPM substep (binning, P2G, grid update, G2P) over the
-whole particle set of the workload.  Default workload: the large sparse
-scene, 16M particles in 64 ellipsoids on a 256^3 grid (elastic/snow, ground
-collider), seeded synthetic inputs.
+A "step" is one MLS-MPM substep (P2G, grid update, G2P, and the binning of
+the substeps that re-sort) over the whole particle set of the workload.
+Default workload: the large sparse scene, 16M particles in 64 ellipsoids on
+a 256^3 grid (elastic/snow, ground collider), seeded synthetic inputs.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
                   [--workload ellipsoids_256|four_materials_128|water_cube_64]
 
-Prints one JSON line.  `value` times K substeps with state resident in HBM
-(CUDA events on the launching stream, barrier + synchronize on both sides,
-max over ranks).  `e2e` runs the drop-in API end to end: read_restart from
-pinned host arrays, step(frame_dt) frames and particle_info() readback.
+Prints one JSON line.  `value` times K substeps with state resident in HBM,
+run as frames through mpm_frame (the kernels MPMSolver.step runs: fused
+G2P+P2G substeps, re-sorted every `resort_every`), with the schedule the
+autotuner measured (CUDA events on the launching stream, barrier +
+synchronize on both sides, max over ranks; events around every launch group
+give the per-kernel times).  `e2e` runs the drop-in API end to end:
+read_restart from pinned host arrays, step(frame_dt) frames and
+particle_info() readback.
 `--impl reference` times the CPU restatement of the reference's substep
 (C/OpenMP float32 oracle, all host threads) on a bounded sample.
 Under torchrun each rank runs an independent replica (replicas only: the
@@ -45,6 +49,12 @@ GRID_BYTES_PER_NODE = 32
 Q_ALGO_BYTES_PER_PARTICLE = 152  # read 76 + write x, v, C, F, Jp 76
 Q_P2G_BYTES_PER_PARTICLE = 100  # read 76 + write F, Jp 24
 KERNELS_PER_SUBSTEP = 10  # 7 binning kernels + p2g + grid + g2p
+FINALIZE_LAUNCHES = 7  # mpm_bin_finalize
+# k_fused does the particle side of one whole substep (the G2P of one substep
+# and the P2G of the next): the per-substep particle figure above, and per
+# node the G2P read and the P2G flush
+FUSED_BYTES_PER_PARTICLE = ALGO_BYTES_PER_PARTICLE
+FUSED_BYTES_PER_NODE = 32
 
 
 def load_peaks():
@@ -167,17 +177,17 @@ def replica_value(units_per_rank, steps, ws, total_ms):
     return units_per_rank * steps * ws / (total_ms / 1e3)
 
 
-def p2g_traffic(n_particles):
-    """k_p2g DRAM bytes per launch: the per-particle figure of the committed
-    ncu capture (profiles/dram_four_materials_128.txt) times the particle
-    count, or None when the summary is absent."""
+def kernel_traffic(kernel, n_particles):
+    """DRAM bytes per launch of `kernel`: the per-particle figure of the
+    committed ncu capture (profiles/dram_four_materials_128.txt) times the
+    particle count, or None when the summary has no figure for it."""
     path = os.path.join(ROOT, "profiles", "dram_four_materials_128.txt")
     if not os.path.exists(path):
         return None
     with open(path) as f:
         for line in f:
             parts = line.split()
-            if len(parts) == 2 and parts[0] == "k_p2g_dram_bytes_per_particle":
+            if len(parts) == 2 and parts[0] == f"{kernel}_dram_bytes_per_particle":
                 return float(parts[1]) * n_particles
     return None
 
@@ -204,22 +214,94 @@ def count_nodes(solver):
     return int((v["grid_vel"][addr, 3] > 0).sum().item())
 
 
+def frame_plan(steps, frame):
+    """Substep counts of the frames that run `steps` substeps."""
+    out = []
+    while steps > 0:
+        out.append(min(frame, steps))
+        steps -= out[-1]
+    return out
+
+
+def frame_launches(count, resort):
+    """Kernel launches of one mpm_frame call: per sort the finalize, P2G and
+    grid update (and the closing G2P of the previous run), per fused substep
+    the fused kernel, two flag passes and the grid update, and the frame's
+    closing G2P."""
+    sorts = (count + resort - 1) // resort
+    return sorts * (FINALIZE_LAUNCHES + 2) + (sorts - 1) + (count - sorts) * 4 + 1
+
+
+def time_frames(solver, dt, plan, stream):
+    """Runs the frames of `plan` through mpm_frame (the kernels of step()),
+    recording CUDA events around every launch group on the launching stream.
+    Returns the events per frame (synchronised)."""
+    import torch
+
+    from taichi_elements_gb300 import _lib
+    evs = []
+    for c in plan:
+        fe = [torch.cuda.Event(enable_timing=True) for _ in range(5 * c + 2)]
+        for e in fe:
+            e.record(stream)  # creates the event
+        evs.append(fe)
+    torch.cuda.synchronize()
+    arrays = [(ctypes.c_void_p * len(fe))(*[e.cuda_event for e in fe]) for fe in evs]
+    if max(plan) > solver._maxv.numel():
+        solver._maxv = torch.zeros(max(plan), dtype=torch.float32, device=solver.device)
+    p = solver.params
+
+    def run():
+        for c, arr in zip(plan, arrays):
+            in_b = ctypes.c_int32(0)
+            _lib.check(solver._lib.mpm_frame(ctypes.byref(p), solver._ws.data_ptr(), solver._cap,
+                                             solver.n_particles, solver._state[solver._cur].data_ptr(),
+                                             solver._state[1 - solver._cur].data_ptr(), float(dt), int(c),
+                                             int(solver.resort_every), solver._maxv.data_ptr(), ctypes.byref(in_b),
+                                             arr, stream.cuda_stream), "mpm_frame")
+            solver._cur = (solver._cur + in_b.value) % 2
+    return evs, run
+
+
+def frame_kernel_times(plan, evs, resort):
+    """Per launch group durations (ms) from the events of time_frames."""
+    out = {"k_p2g": [], "k_fused": [], "k_g2p_stream": [], "binning": [], "grid": []}
+    for c, ev in zip(plan, evs):
+        def t(i, j):
+            return ev[i].elapsed_time(ev[j])
+        for k in range(c):
+            b = 5 * k
+            if k % resort == 0:
+                if k > 0:
+                    out["k_g2p_stream"].append(t(b, b + 1))
+                out["binning"].append(t(b + 1, b + 2))
+                out["k_p2g"].append(t(b + 2, b + 3))
+            else:
+                out["k_fused"].append(t(b + 2, b + 3))
+            out["grid"].append(t(b + 3, b + 4))
+        out["k_g2p_stream"].append(t(5 * c, 5 * c + 1))
+    return out
+
+
 def run_gb300(args):
     import torch
 
     from taichi_elements_gb300 import _lib
-    from taichi_elements_gb300.mpm_solver import MPMSolver
 
     ws, rank, local = dist_init()
     sc = make_scene(args.workload)
     skw = dict(quant=True) if args.quant else {}
     solver = sc.make_solver(chunk=args.chunk, **skw) if args.chunk else sc.make_solver(**skw)
+    solver.use_cuda_graph = False  # events between launches; the graph replays the same kernels
     dt = sc.default_dt
-    chunk_times = None
-    if not args.chunk:
-        from taichi_elements_gb300.autotune import time_chunks, tune_chunk
-        chunk_times = time_chunks(solver)
-        tune_chunk(solver)
+    tuned = None
+    if args.chunk is None and args.resort is None:
+        from taichi_elements_gb300.autotune import tune_schedule
+        tuned = tune_schedule(solver)
+    if args.resort is not None:
+        solver.resort_every = args.resort
+        solver.fuse_frames = True
+    fused = solver._fuses_frames
     lib = solver._lib
     stream = torch.cuda.current_stream()
     sptr = stream.cuda_stream
@@ -247,22 +329,31 @@ def run_gb300(args):
         solver._cur = 1 - solver._cur
 
     solver._prepare(dt * (args.steps + args.warmup))
-    for _ in range(args.warmup):
-        substep_phases()
+    plan = frame_plan(args.steps, args.frame)
+    if fused:
+        _, warm = time_frames(solver, dt, [args.warmup], stream)
+        warm()
+        evs, run = time_frames(solver, dt, plan, stream)
+    else:
+        for _ in range(args.warmup):
+            substep_phases()
+        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(5)] for _ in range(args.steps)]
+
+        def run():
+            for k in range(args.steps):
+                substep_phases(evs[k])
     torch.cuda.synchronize()
     n_nodes = count_nodes(solver)
     occupancy = block8_fraction(solver)
 
-    # timed region: K substeps, per-phase CUDA events on the launching stream
-    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(5)] for _ in range(args.steps)]
+    # timed region: K substeps, CUDA events on the launching stream
     start = torch.cuda.Event(enable_timing=True)
     stop = torch.cuda.Event(enable_timing=True)
     barrier(ws)
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
         start.record(stream)
-        for k in range(args.steps):
-            substep_phases(evs[k])
+        run()
         stop.record(stream)
         torch.cuda.synchronize()
     barrier(ws)
@@ -270,23 +361,42 @@ def run_gb300(args):
     st = int(solver._status.item())
     if st:
         raise RuntimeError(f"device status {st} during the benchmark")
-    ph = np.array([[e[i].elapsed_time(e[i + 1]) for i in range(4)] for e in evs])
-    ph_mean = ph.mean(0)
     n = solver.n_particles
     value = replica_value(n, args.steps, ws, total_ms)
     peak, peak_kind = load_peaks()
-    per_p2g = Q_P2G_BYTES_PER_PARTICLE if args.quant else P2G_BYTES_PER_PARTICLE
-    per_sub = Q_ALGO_BYTES_PER_PARTICLE if args.quant else ALGO_BYTES_PER_PARTICLE
-    p2g_bytes = per_p2g * n + P2G_BYTES_PER_NODE * n_nodes
-    p2g_ach = p2g_bytes / (ph_mean[1] / 1e3) / 1e9
-    sub_bytes = per_sub * n + ALGO_BYTES_PER_NODE * n_nodes
-    sub_ach = sub_bytes / ((ph_mean[1] + ph_mean[2] + ph_mean[3]) / 1e3) / 1e9
-    full_ach = sub_bytes / (ph.sum(1).mean() / 1e3) / 1e9
-    traffic = None if args.quant else p2g_traffic(n)
-
+    sub_bytes = (Q_ALGO_BYTES_PER_PARTICLE if args.quant else ALGO_BYTES_PER_PARTICLE) * n + \
+        ALGO_BYTES_PER_NODE * n_nodes
+    if fused:
+        kt = frame_kernel_times(plan, evs, solver.resort_every)
+        launches = sum(frame_launches(c, solver.resort_every) for c in plan)
+        totals = {k: float(sum(v)) for k, v in kt.items()}
+        phases = {k: totals[k] / args.steps for k in totals}
+        per_launch = {k: (totals[k] / len(v) if v else 0.0) for k, v in kt.items()}
+        kernel_bytes = {"k_fused": FUSED_BYTES_PER_PARTICLE * n + FUSED_BYTES_PER_NODE * n_nodes,
+                        "k_p2g": P2G_BYTES_PER_PARTICLE * n + P2G_BYTES_PER_NODE * n_nodes,
+                        "k_g2p_stream": G2P_BYTES_PER_PARTICLE * n + G2P_BYTES_PER_NODE * n_nodes}
+        top = max(kernel_bytes, key=lambda k: totals[k])
+        schedule = {"mode": "fused frames (mpm_frame)", "resort_every": solver.resort_every,
+                    "frames": plan, "launches_per_kernel": {k: len(v) for k, v in kt.items()},
+                    "ms_per_launch": per_launch}
+    else:
+        ph = np.array([[e[i].elapsed_time(e[i + 1]) for i in range(4)] for e in evs])
+        launches = KERNELS_PER_SUBSTEP * args.steps
+        phases = dict(zip(("binning", "k_p2g", "grid", "k_g2p"), ph.mean(0)))
+        per_launch = dict(phases)
+        totals = {k: v * args.steps for k, v in phases.items()}
+        per_p2g = Q_P2G_BYTES_PER_PARTICLE if args.quant else P2G_BYTES_PER_PARTICLE
+        kernel_bytes = {"k_p2g": per_p2g * n + P2G_BYTES_PER_NODE * n_nodes}
+        top = "k_p2g"
+        schedule = {"mode": "per-substep launches (mpm_substep phases)", "chunk": solver.chunk}
+    top_ach = kernel_bytes[top] / (per_launch[top] / 1e3) / 1e9
+    no_bin_ms = (total_ms - totals["binning"]) / args.steps
+    sub_ach = sub_bytes / (no_bin_ms / 1e3) / 1e9
+    full_ach = sub_bytes / (total_ms / args.steps / 1e3) / 1e9
+    traffic = None if args.quant else kernel_traffic(top, n)
     e2e = None
     if not args.no_e2e:
-        e2e = run_e2e(sc, args, ws)
+        e2e = run_e2e(sc, args, ws, (solver.fuse_frames, solver.resort_every, solver.chunk))
     batched = None
     if not args.no_batched:
         batched = run_batched_measure()
@@ -332,17 +442,19 @@ def run_gb300(args):
             "l2": f"inputs larger than L2: particle state {n * 212 / 1e9:.2f} GB per buffer pair",
             "parallelism": f"replicas x{ws}",
             "chunk": solver.chunk,
-            "chunk_ms_per_substep": chunk_times,
+            "autotune": tuned,
         },
-        "phases_ms": {"binning": ph_mean[0], "p2g": ph_mean[1], "grid": ph_mean[2], "g2p": ph_mean[3]},
-        "roofline": {"bound": "hbm", "kernel": "k_p2g", "achieved": p2g_ach, "peak": peak, "unit": "GB/s",
-                     "frac": p2g_ach / peak, "traffic": traffic,
-                     "algorithmic_bytes_per_launch": p2g_bytes, "peak_source": peak_kind},
-        "roofline_substep": {"bound": "hbm", "kernels": "p2g+grid+g2p", "achieved": sub_ach, "peak": peak,
+        "schedule": schedule,
+        "phases_ms_per_substep": phases,
+        "roofline": {"bound": "hbm", "kernel": top, "achieved": top_ach, "peak": peak, "unit": "GB/s",
+                     "frac": top_ach / peak, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": kernel_bytes[top], "ms_per_launch": per_launch[top],
+                     "peak_source": peak_kind},
+        "roofline_substep": {"bound": "hbm", "kernels": "all but binning", "achieved": sub_ach, "peak": peak,
                              "unit": "GB/s", "frac": sub_ach / peak,
                              "with_binning": {"achieved": full_ach, "frac": full_ach / peak},
                              "algorithmic_bytes_per_substep": sub_bytes, "peak_source": peak_kind},
-        "gpu_launches": KERNELS_PER_SUBSTEP * args.steps,
+        "gpu_launches": launches,
         "clocks": clk.summary(),
         "e2e": e2e,
         "cpu_baseline": cpu,
@@ -359,9 +471,10 @@ def run_gb300(args):
         print(json.dumps(line))
 
 
-def run_e2e(sc, args, ws):
+def run_e2e(sc, args, ws, schedule):
     """End to end through the drop-in API: pinned host arrays -> read_restart
-    -> step(frame_dt) frames -> particle_info()."""
+    -> step(frame_dt) frames -> particle_info(), with the schedule of the
+    timed substeps (fuse_frames, resort_every, chunk)."""
     import torch
 
     from taichi_elements_gb300.mpm_solver import MPMSolver
@@ -374,7 +487,8 @@ def run_e2e(sc, args, ws):
     count, _ = MPMSolver.count_substeps(frame_dt, sc.default_dt)
 
     def once(timed):
-        s = MPMSolver(sc.res, size=sc.size)
+        s = MPMSolver(sc.res, size=sc.size, chunk=schedule[2])
+        s.fuse_frames, s.resort_every = schedule[0], schedule[1]
         for cc in sc.postprocess:
             s.add_surface_collider(cc["point"], cc["normal"], cc.get("surface", 0), cc.get("friction", 0.0))
         torch.cuda.synchronize()
@@ -817,6 +931,8 @@ def main():
     ap.add_argument("--workload", default="ellipsoids_256",
                     choices=["ellipsoids_256", "four_materials_128", "water_cube_64", "elastic_on_water"])
     ap.add_argument("--chunk", type=int, default=None)
+    ap.add_argument("--resort", type=int, default=None, help="fused frames re-sorted every this many substeps")
+    ap.add_argument("--frame", type=int, default=50, help="substeps per mpm_frame call in the timed region")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")

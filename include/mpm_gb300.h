@@ -183,10 +183,16 @@ int mpm_substep(const MpmParams *p, void *ws, int64_t cap, int64_t n, const floa
  * mpm_frame on it); both buffers satisfy mpm_p2g's layout rules; no
  * quantized state, no batch (n_scenes == 0).  `maxv` receives the max |v|
  * after each substep (count floats).  On return `*in_b` is 1 when the state
- * ends in `b`, 0 when in `a`.  No single counterpart in the reference, whose
- * loop launches the four kernels of each substep separately. */
+ * ends in `b`, 0 when in `a`.  `events` is NULL, or 5 * count + 2 cudaEvent_t
+ * recorded on the stream for timing: events[5k .. 5k+4] at substep k's start,
+ * after the previous run's closing G2P (a sort substep; else at once), after
+ * the finalize (likewise), after the particle kernel (P2G of a sort, or the
+ * fused G2P+P2G) and after the grid update; events[5 count] and
+ * [5 count + 1] bracket the frame's closing G2P.  No single counterpart in
+ * the reference, whose loop launches the four kernels of each substep
+ * separately. */
 int mpm_frame(const MpmParams *p, void *ws, int64_t cap, int64_t n, float *a, float *b, float dt, int32_t count,
-              int32_t resort, float *maxv, int32_t *in_b, void *stream);
+              int32_t resort, float *maxv, int32_t *in_b, void *const *events, void *stream);
 
 /* One substep of the fused G2P2G mode (MPMSolver(use_g2p2g=True),
  * engine/mpm_solver.py:363-485 and :773-787): G2P from the grid velocities of

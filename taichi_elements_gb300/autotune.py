@@ -1,14 +1,25 @@
-"""Measured choice of the P2G/G2P work-item size (particles per CTA item).
+"""Measured choice of the substep schedule.
 
-The engine splits each active 4^3 grid block's particles into work items of
-`chunk` particles; one CTA processes one item with its shared-memory tiles.
-Large items amortise the tile flush, small items give a small scene enough
-CTAs to fill 152 SMs.  ``tune_chunk`` times a few substeps for each candidate
-on a scratch copy of the solver's particles (the simulation itself is not
-advanced) and keeps the fastest.  Results are cached in memory per
-(device, particle-count bucket, grid resolution, per-particle E), and in the
-JSON file named by the MPM_GB300_TUNE_CACHE environment variable when it is
-set.
+Two schedules run the reference's plain substep loop with the same
+arithmetic:
+
+* per-substep launches (mpm_substep): every substep sorts the particles by
+  grid block, and G2P stages each block's 6^3 velocity halo in shared memory.
+  The engine splits each active 4^3 grid block's particles into work items of
+  `chunk` particles; large items amortise the halo staging, small items give
+  a small scene enough CTAs to fill 152 SMs.
+* fused frames (mpm_frame): the particles are re-sorted every `resort`
+  substeps; in between, the G2P of one substep (velocity gathers through L1,
+  no halo staging) and the P2G of the next run as one kernel.  Frequent sorts
+  keep the scatter tiles dense; rare sorts save the sort's data movement.
+
+``tune_chunk`` times the chunk candidates; ``tune_schedule`` times fused
+frames for each re-sort candidate against the per-substep schedule at its
+best chunk and applies the fastest.  Both run on a scratch copy of the
+solver's particles (the simulation itself is not advanced).  Results are
+cached in memory per (device, particle-count bucket, grid resolution,
+per-particle E, material mix), and in the JSON file named by the
+MPM_GB300_TUNE_CACHE environment variable when it is set.
 """
 from __future__ import annotations
 
@@ -23,14 +34,26 @@ import torch
 from . import _lib
 
 CANDIDATES = (128, 256, 512, 1024)
+RESORT_CANDIDATES = (2, 4, 8, 16)
 _cache: dict = {}
 _lock = threading.Lock()
 
 
-def _key(solver) -> str:
+def material_mix(solver) -> str:
+    """The materials present, as a string of material ids ("013")."""
+    n = solver.n_particles
+    if n == 0 or solver.quant:
+        return "-"
+    m = solver._state[solver._cur][_lib.ROW_MAT, :n].view(torch.int32) & 0xFF
+    present = torch.bincount(m.long(), minlength=8)[:8].cpu().numpy()
+    return "".join(str(k) for k in range(8) if present[k] > 0)
+
+
+def _key(solver, what="chunk") -> str:
     dev = torch.cuda.get_device_name(solver.device)
     bucket = int(math.log2(max(solver.n_particles, 1)))
-    return f"{dev}|{bucket}|{'x'.join(map(str, solver.res))}|{int(solver.per_particle_E)}"
+    key = f"{dev}|{bucket}|{'x'.join(map(str, solver.res))}|{int(solver.per_particle_E)}"
+    return key if what == "chunk" else f"{what}|{key}|{material_mix(solver)}"
 
 
 def _load_file():
@@ -107,3 +130,73 @@ def tune_chunk(solver, candidates=CANDIDATES, substeps=8) -> int:
         solver.chunk = int(best)
         solver._invalidate_params()
     return int(best)
+
+
+def time_frames(solver, candidates=RESORT_CANDIDATES, substeps=24, dt=None):
+    """Milliseconds per substep of a fused frame of `substeps` substeps for
+    each re-sort interval, measured on a copy."""
+    solver._prepare(dt or solver.default_dt)
+    dt = float(dt or solver.default_dt)
+    lib = solver._lib
+    n, cap = solver.n_particles, solver._cap
+    bufs = [torch.empty_like(solver._state[0]), torch.empty_like(solver._state[0])]
+    ws = torch.empty_like(solver._ws)
+    maxv = torch.zeros(substeps, dtype=torch.float32, device=solver.device)
+    stream = torch.cuda.current_stream(solver.device)
+    p = _lib.MpmParams.from_buffer_copy(solver.params)
+    pp = ctypes.byref(p)
+    out = {}
+    for r in candidates:
+        bufs[0].copy_(solver._state[solver._cur])
+        _lib.check(lib.mpm_workspace_init(pp, ws.data_ptr(), cap, stream.cuda_stream), "mpm_workspace_init")
+        _lib.check(lib.mpm_bin_count(pp, ws.data_ptr(), cap, bufs[0].data_ptr(), 0, n, stream.cuda_stream),
+                   "mpm_bin_count")
+        cur = 0
+
+        def frame():
+            nonlocal cur
+            in_b = ctypes.c_int32(0)
+            _lib.check(lib.mpm_frame(pp, ws.data_ptr(), cap, n, bufs[cur].data_ptr(), bufs[1 - cur].data_ptr(),
+                                     dt, substeps, int(r), maxv.data_ptr(), ctypes.byref(in_b), None,
+                                     stream.cuda_stream), "mpm_frame")
+            cur = (cur + in_b.value) % 2
+
+        frame()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        frame()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out[int(r)] = e0.elapsed_time(e1) / substeps
+    return out
+
+
+def tune_schedule(solver, resort_candidates=RESORT_CANDIDATES, chunk_candidates=CANDIDATES, substeps=24) -> dict:
+    """Measure fused frames for each re-sort interval and per-substep
+    launches for each chunk, apply the fastest (solver.fuse_frames,
+    solver.resort_every, solver.chunk) and return the choice with the
+    measured milliseconds per substep."""
+    with _lock:
+        if not _cache:
+            _load_file()
+        key = _key(solver, "schedule")
+        best = _cache.get(key)
+    if best is None:
+        chunks = time_chunks(solver, chunk_candidates, substeps=8)
+        chunk = min(chunks, key=chunks.get)
+        frames = {} if solver.quant or solver.use_g2p2g else time_frames(solver, resort_candidates, substeps)
+        best = {"chunk": int(chunk), "substep_ms": {str(c): t for c, t in chunks.items()},
+                "frame_ms": {str(r): t for r, t in frames.items()}}
+        if frames and min(frames.values()) < chunks[chunk]:
+            best.update(mode="frame", resort=int(min(frames, key=frames.get)))
+        else:
+            best.update(mode="substep", resort=int(solver.resort_every))
+        with _lock:
+            _cache[key] = best
+            _save_file()
+    solver.fuse_frames = best["mode"] == "frame"
+    solver.resort_every = int(best["resort"])
+    if solver.chunk != best["chunk"]:
+        solver.chunk = int(best["chunk"])
+        solver._invalidate_params()
+    return dict(best, key=key)

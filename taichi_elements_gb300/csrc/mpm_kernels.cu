@@ -1068,16 +1068,15 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_fused(const M
     if (act) {
       // G2P of the previous substep, :694-724
       const Base b0 = particle_base(P, x[0], x[1], x[2], bad_b);
+      // v and C feed this P2G only: the next substep gathers them afresh and
+      // the frame's closing G2P (k_g2p_stream) stores the final ones
       if (mat != 4) {
         gather_vc(P, w.grid_vel, b0, v, C);
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-          st[(R::V + d) * cap + i] = v[d];
           x[d] = x[d] + dt * v[d];
           st[(R::X + d) * cap + i] = x[d];
         }
-#pragma unroll
-        for (int a = 0; a < 9; ++a) st[(R::C + a) * cap + i] = C[a / 3][a % 3];
       } else {  // stationary: v, C and x stay
 #pragma unroll
         for (int d = 0; d < 3; ++d) v[d] = st[(R::V + d) * cap + i];
@@ -1768,8 +1767,10 @@ int mpm_substep(const MpmParams *p, void *ws, int64_t cap, int64_t n, const floa
 // One fused substep on `st` in place: G2P of the previous substep and P2G
 // of this one (k_fused), the grid-active list from the flagged blocks, the
 // grid update.
-static int fused_substep(const DevInfo *di, cudaStream_t s, const MpmParams &p, const Ws &w, float *st, int64_t cap,
-                         int64_t n, float dt, float *maxv) {
+// The particle kernel of a fused substep: G2P of the previous substep,
+// advection, constitutive update and P2G, in place on `st`.
+static int fused_particles(const DevInfo *di, cudaStream_t s, const MpmParams &p, const Ws &w, float *st, int64_t cap,
+                           int64_t n, float dt, float *maxv) {
   CUtensorMap mx, mf;
   const int nf = p.has_Ep ? kFusedRowsF : kFusedRowsF - 2;
   if (!rows_tensor_map(&mx, st, cap, MPM_NROWS, 3) || !rows_tensor_map(&mf, st, cap, MPM_NROWS, nf))
@@ -1778,10 +1779,15 @@ static int fused_substep(const DevInfo *di, cudaStream_t s, const MpmParams &p, 
     k_fused<true><<<di->fused_ep_ctas, kP2GThreads, kFusedSmem, s>>>(p, w, mx, mf, st, cap, n, dt, maxv);
   else
     k_fused<false><<<di->fused_ctas, kP2GThreads, kFusedSmem, s>>>(p, w, mx, mf, st, cap, n, dt, maxv);
+  return MPM_OK;
+}
+
+// The grid half of a fused substep: the blocks the particles marked become
+// the grid-active list, then the grid update over them.
+static void fused_grid(cudaStream_t s, const DevInfo *di, const MpmParams &p, const Ws &w, float dt) {
   k_flags_count<<<w.nflagtiles, 256, 0, s>>>(p, w);
   k_flags_write<<<w.nflagtiles, 256, 0, s>>>(p, w);
   k_grid<false><<<di->sms * 8, 256, 0, s>>>(p, nullptr, w, dt);
-  return last_error();
 }
 
 static bool batch_ok(const MpmParams *p) {
@@ -1863,7 +1869,7 @@ int mpm_substep_noalloc(const MpmParams *p, int64_t cap, int64_t n, const float 
 }
 
 int mpm_frame(const MpmParams *p, void *ws, int64_t cap, int64_t n, float *a, float *b, float dt, int32_t count,
-              int32_t resort, float *maxv, int32_t *in_b, void *stream) {
+              int32_t resort, float *maxv, int32_t *in_b, void *const *events, void *stream) {
   if (!params_ok(p) || p->quant || p->n_scenes > 0 || !ws || !a || !b || !maxv || !in_b || n < 0 || n > cap ||
       count < 1 || resort < 1 || !p2g_rows_ok(a, cap) || !p2g_rows_ok(b, cap))
     return MPM_E_INVALID;
@@ -1872,27 +1878,46 @@ int mpm_frame(const MpmParams *p, void *ws, int64_t cap, int64_t n, float *a, fl
   Ws w;
   ws_layout(*p, cap, (char *)ws, &w);
   cudaStream_t s = (cudaStream_t)stream;
+  // events[5k + j]: substep k's start, after the closing G2P of the previous
+  // sort run, after the finalize, after the particle kernel, after the grid
+  // update; events[5 count], [5 count + 1] bracket the frame's last G2P
+  auto mark = [&](int64_t e) {
+    if (events) cudaEventRecord((cudaEvent_t)events[e], s);
+  };
   float *cur = a, *oth = b;
   int rc = MPM_OK;
   for (int k = 0; k < count; ++k) {
+    mark(5 * k);
     if (k % resort == 0) {
       // close the previous substep with the binning of this sort, then sort
       if (k > 0 && n > 0)
         k_g2p_stream<<<di->g2ps_ctas, 128, 0, s>>>(*p, w, cur, cap, n, dt, maxv + k - 1);
+      mark(5 * k + 1);
       rc = mpm_bin_finalize(p, ws, cap, n, stream);
       if (rc) return rc;
+      mark(5 * k + 2);
       rc = launch_p2g_single(di, s, *p, w, cur, oth, cap, n, dt);
       if (rc) return rc;
+      mark(5 * k + 3);
       k_grid<false><<<di->sms * 8, 256, 0, s>>>(*p, nullptr, w, dt);
       float *t = cur;
       cur = oth;
       oth = t;
-    } else if (n > 0) {
-      rc = fused_substep(di, s, *p, w, cur, cap, n, dt, maxv + k - 1);
-      if (rc) return rc;
+    } else {
+      mark(5 * k + 1);
+      mark(5 * k + 2);
+      if (n > 0) {
+        rc = fused_particles(di, s, *p, w, cur, cap, n, dt, maxv + k - 1);
+        if (rc) return rc;
+      }
+      mark(5 * k + 3);
+      if (n > 0) fused_grid(s, di, *p, w, dt);
     }
+    mark(5 * k + 4);
   }
+  mark(5 * (int64_t)count);
   if (n > 0) k_g2p_stream<<<di->g2ps_ctas, 128, 0, s>>>(*p, w, cur, cap, n, dt, maxv + count - 1);
+  mark(5 * (int64_t)count + 1);
   *in_b = cur == b;
   return last_error();
 }

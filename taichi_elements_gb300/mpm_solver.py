@@ -18,7 +18,9 @@ Extensions beyond the reference: ``substep(dt)``, per-particle Young's
 modulus (``per_particle_E=True`` and the ``E`` argument of the seeding
 calls), ``state_dict``/``load_state_dict`` (exact checkpoints of x, v, C, F,
 Jp), ``tensors()`` (zero-copy device views), CUDA-graph capture of whole
-frames and a measured choice of the work-item size (``autotune=True``).
+frames, fused frames (the G2P of one substep and the P2G of the next in one
+kernel, ``fuse_frames``) and a measured choice of the substep schedule
+(``autotune=True``).
 
 ``quant=True`` keeps the particles in the packed layout of the reference's
 quantized fields (engine/mpm_solver.py:106-127, :216-262): positions as
@@ -168,8 +170,10 @@ class MPMSolver:
         self.writers = []
 
         self.per_particle_E = bool(per_particle_E)
-        # fused frames re-sort the particles by grid block every this many
-        # substeps (the storage order drifts from the positions in between)
+        # frames run fused (mpm_frame), re-sorting the particles by grid block
+        # every `resort_every` substeps (the storage order drifts from the
+        # positions in between); autotune.tune_schedule measures both choices
+        self.fuse_frames = True
         self.resort_every = 8
         self.chunk = int(chunk) if chunk else self.DEFAULT_CHUNK
         self.use_cuda_graph = use_cuda_graph
@@ -743,7 +747,7 @@ class MPMSolver:
     def _fuses_frames(self) -> bool:
         """Frames of the plain substep run as fused substeps (mpm_frame):
         float32 storage and the reference's plain loop (not use_g2p2g)."""
-        return not self.quant and not self.use_g2p2g
+        return self.fuse_frames and not self.quant and not self.use_g2p2g
 
     def _launch_frame(self, count: int, dt: float):
         """All substeps of a frame: the plain loop fused (G2P of one substep
@@ -753,7 +757,7 @@ class MPMSolver:
         _lib.check(
             self._lib.mpm_frame(ctypes.byref(p), _ptr(self._ws), self._cap, self.n_particles,
                                 _ptr(self._state[self._cur]), _ptr(self._state[1 - self._cur]), float(dt), int(count),
-                                int(self.resort_every), _ptr(self._maxv), ctypes.byref(in_b), self.stream),
+                                int(self.resort_every), _ptr(self._maxv), ctypes.byref(in_b), None, self.stream),
             "mpm_frame")
         self._cur = (self._cur + int(in_b.value)) % 2
 
@@ -774,7 +778,7 @@ class MPMSolver:
         if count > self._maxv.numel():
             self._maxv = torch.zeros(count, dtype=torch.float32, device=self.device)
         key = (count, float(dt), self._cur, self.n_particles, self._params_version, _ptr(self._ws),
-               self.resort_every)
+               self._fuses_frames, self.resort_every)
         if self.use_g2p2g:  # the first substep's launch depends on the mode's state
             key += (bool(self._g2p2g_listed), self._last_final if self._g2p2g_grid_valid else 0)
         if not self.use_cuda_graph:
@@ -805,8 +809,8 @@ class MPMSolver:
             print(f'needed substeps: {int(frame_dt / self.default_dt) + 1}')
         self._prepare(frame_dt)
         if self.autotune and not self._tuned and self.n_particles > 0:
-            from .autotune import tune_chunk
-            tune_chunk(self)
+            from .autotune import tune_schedule
+            tune_schedule(self)
             self._tuned = True
         if self.use_adaptive_dt:
             self._host_box = None

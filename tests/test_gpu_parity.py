@@ -304,6 +304,25 @@ def test_autotune_picks_a_candidate_and_leaves_state_untouched():
     assert np.abs(s.particle_info()['position'] - ref.particle_info()['position']).max() < 1e-5
 
 
+def test_schedule_autotune_applies_a_measured_choice_and_leaves_state_untouched():
+    from taichi_elements_gb300.autotune import CANDIDATES, RESORT_CANDIDATES, tune_schedule
+    sc = scenes.smoke_scene()
+    s = sc.make_solver()
+    before = s.full_state()['x'].clone()
+    choice = tune_schedule(s)
+    assert choice["mode"] in ("frame", "substep") and choice["chunk"] in CANDIDATES
+    assert set(map(int, choice["frame_ms"])) == set(RESORT_CANDIDATES)
+    assert s.fuse_frames == (choice["mode"] == "frame") and s.chunk == choice["chunk"]
+    if s.fuse_frames:
+        assert s.resort_every == choice["resort"]
+    assert torch.equal(s.full_state()['x'], before)
+    s.step(2e-3)
+    ref = sc.make_solver(chunk=512)
+    ref.fuse_frames = False
+    ref.step(2e-3)
+    assert np.abs(s.particle_info()['position'] - ref.particle_info()['position']).max() < 1e-5
+
+
 def test_adaptive_dt_frames_match_oracle_with_the_same_steps():
     """use_adaptive_dt=True (engine/mpm_solver.py:756-766): each substep's dt
     is min(dt, 0.9 dx / (max grid |v| + 1e-6), time left), the frame's dts

@@ -26,6 +26,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes
+import gc
 import json
 import os
 import statistics
@@ -295,12 +296,13 @@ def run_gb300(args):
     solver.use_cuda_graph = False  # events between launches; the graph replays the same kernels
     dt = sc.default_dt
     tuned = None
-    if args.chunk is None and args.resort is None:
+    if args.chunk is None and args.resort is None and args.schedule is None:
         from taichi_elements_gb300.autotune import tune_schedule
         tuned = tune_schedule(solver)
     if args.resort is not None:
         solver.resort_every = args.resort
-        solver.fuse_frames = True
+    if args.schedule is not None:
+        solver.fuse_frames = args.schedule == "frame"
     fused = solver._fuses_frames
     lib = solver._lib
     stream = torch.cuda.current_stream()
@@ -494,22 +496,35 @@ def run_e2e(sc, args, ws, schedule):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         s.read_restart(sc.n, x.numpy(), v.numpy(), m.numpy(), c.numpy())
-        outs = []
+        t1 = time.perf_counter()
+        outs, parts = [], []
         for _ in range(frames):
+            a = time.perf_counter()
             s.step(frame_dt)
+            b = time.perf_counter()
             outs.append(s.particle_info())
+            parts.append((b - a, time.perf_counter() - b))
         torch.cuda.synchronize()
-        return time.perf_counter() - t0
+        t = time.perf_counter() - t0
+        del s, outs
+        gc.collect()
+        return t, t1 - t0, parts
 
-    once(False)  # warm-up: library, allocations, CUDA-graph capture
+    # warm-up: library, allocations, CUDA-graph capture, page-locked host
+    # buffers (the caching host allocator keeps them for the timed run)
+    once(False)
+    once(False)
     barrier(ws)
-    t = allmax(once(True), ws)
+    t, t_read, parts = once(True)
+    t = allmax(t, ws)
     h2d = sc.n * (12 + 12 + 4 + 4)
     d2h = sc.n * (12 + 12 + 4 + 4)
     return {"value": sc.n * count * frames * ws / t, "unit": "particle-substeps/s",
             "h2d_bytes_per_step": h2d / frames, "d2h_bytes_per_step": d2h,
             "step": f"one step(frame_dt) frame of {count} substeps + particle_info(); read_restart of the scene "
                     f"from pinned host memory inside the timed region (amortised over {frames} frames)",
+            "ms": {"read_restart": 1e3 * t_read, "step": [1e3 * a for a, _ in parts],
+                   "particle_info": [1e3 * b for _, b in parts]},
             "frames": frames, "seconds": t}
 
 
@@ -933,6 +948,8 @@ def main():
     ap.add_argument("--chunk", type=int, default=None)
     ap.add_argument("--resort", type=int, default=None, help="fused frames re-sorted every this many substeps")
     ap.add_argument("--frame", type=int, default=50, help="substeps per mpm_frame call in the timed region")
+    ap.add_argument("--schedule", choices=["frame", "substep"], default=None,
+                    help="fused frames or per-substep launches (default: the autotuner's choice)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")

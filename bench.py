@@ -255,18 +255,32 @@ def time_frames(solver, dt, plan, stream):
     def run():
         for c, arr in zip(plan, arrays):
             in_b = ctypes.c_int32(0)
-            _lib.check(solver._lib.mpm_frame(ctypes.byref(p), solver._ws.data_ptr(), solver._cap,
-                                             solver.n_particles, solver._state[solver._cur].data_ptr(),
-                                             solver._state[1 - solver._cur].data_ptr(), float(dt), int(c),
-                                             int(solver.resort_every), solver._maxv.data_ptr(), ctypes.byref(in_b),
-                                             arr, stream.cuda_stream), "mpm_frame")
+            a = solver._state[solver._cur].data_ptr()
+            b = solver._state[1 - solver._cur].data_ptr()
+            if solver.use_g2p2g:  # every particle took part in the previous substep
+                _lib.check(solver._lib.mpm_g2p2g_frame(ctypes.byref(p), solver._ws.data_ptr(), solver._cap,
+                                                       solver.n_particles, a, b, float(dt), int(c),
+                                                       int(solver.resort_every), solver.n_particles,
+                                                       solver._maxv.data_ptr(), ctypes.byref(in_b), arr,
+                                                       stream.cuda_stream), "mpm_g2p2g_frame")
+            else:
+                _lib.check(solver._lib.mpm_frame(ctypes.byref(p), solver._ws.data_ptr(), solver._cap,
+                                                 solver.n_particles, a, b, float(dt), int(c),
+                                                 int(solver.resort_every), solver._maxv.data_ptr(),
+                                                 ctypes.byref(in_b), arr, stream.cuda_stream), "mpm_frame")
             solver._cur = (solver._cur + in_b.value) % 2
     return evs, run
 
 
-def frame_kernel_times(plan, evs, resort):
-    """Per launch group durations (ms) from the events of time_frames."""
-    out = {"k_p2g": [], "k_fused": [], "k_g2p_stream": [], "binning": [], "grid": []}
+def frame_kernel_times(plan, evs, resort, g2p2g=False):
+    """Per launch group durations (ms) from the events of time_frames.  Plain
+    frames: the sort's P2G (k_p2g), the fused substeps (k_fused), the closing
+    G2P that also bins (k_g2p_stream); G2P2G frames: the sorting pass
+    (k_fused_sorted), the in-place substeps (k_fused) and the binning passes
+    (k_bin_box).  "binning" is the sorts' finalize, "grid" the grid update
+    with the flag passes."""
+    sort_k, bin_k = ("k_fused_sorted", "k_bin_box") if g2p2g else ("k_p2g", "k_g2p_stream")
+    out = {sort_k: [], "k_fused": [], bin_k: [], "binning": [], "grid": []}
     for c, ev in zip(plan, evs):
         def t(i, j):
             return ev[i].elapsed_time(ev[j])
@@ -274,13 +288,13 @@ def frame_kernel_times(plan, evs, resort):
             b = 5 * k
             if k % resort == 0:
                 if k > 0:
-                    out["k_g2p_stream"].append(t(b, b + 1))
+                    out[bin_k].append(t(b, b + 1))
                 out["binning"].append(t(b + 1, b + 2))
-                out["k_p2g"].append(t(b + 2, b + 3))
+                out[sort_k].append(t(b + 2, b + 3))
             else:
                 out["k_fused"].append(t(b + 2, b + 3))
             out["grid"].append(t(b + 3, b + 4))
-        out["k_g2p_stream"].append(t(5 * c, 5 * c + 1))
+        out[bin_k].append(t(5 * c, 5 * c + 1))
     return out
 
 
@@ -410,7 +424,7 @@ def run_gb300(args):
         render = run_render_measure(solver, rank == 0 and not args.no_cpu)
     g2p2g = None
     if not args.no_g2p2g:
-        g2p2g = run_g2p2g_measure(sc)
+        g2p2g = run_g2p2g_measure(sc, solver.resort_every)
     quant = None
     if not args.no_quant:
         quant = run_quant_measure(sc)
@@ -689,29 +703,48 @@ def run_quant_measure(sc, substeps=50):
     return out
 
 
-def run_g2p2g_measure(sc, substeps=50, warmup=5):
+def run_g2p2g_measure(sc, resort, substeps=50, warmup=5):
     """The same scene in the fused G2P2G mode (MPMSolver(use_g2p2g=True),
-    engine/mpm_solver.py:363-485): K substeps timed with CUDA events."""
+    engine/mpm_solver.py:363-485): K substeps as one frame through
+    mpm_g2p2g_frame (what step() runs, re-sorted every `resort` substeps),
+    then K substeps of per-substep launches (substep() and the adaptive-dt
+    loop), each timed with CUDA events."""
     import torch
     s = sc.make_solver(use_g2p2g=True, chunk=512)
+    s.use_cuda_graph = False
+    s.resort_every = resort
     dt = sc.default_dt
     s._prepare(dt)
+    s._maxv = torch.zeros(max(substeps, warmup), dtype=torch.float32, device=s.device)
+    stream = torch.cuda.current_stream()
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / substeps
+
+    s._launch_substeps(warmup, dt)  # the first frame: fresh particles, the mode's state
+    evs, run = time_frames(s, dt, [substeps], stream)
+    ms_frame = timed(run)
+    kt = frame_kernel_times([substeps], evs, resort, g2p2g=True)
+    s.fuse_frames = False
+    s._g2p2g_listed = 0  # time_frames left the state binned (counts), as a frame does
     for _ in range(warmup):
         s._launch_substep(dt, -1)
-    stream = torch.cuda.current_stream()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(substeps):
-        s._launch_substep(dt, -1)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / substeps
+    ms_sub = timed(lambda: [s._launch_substep(dt, -1) for _ in range(substeps)])
     if int(s._status.item()):
         raise RuntimeError("device status set during the G2P2G measurement")
     n = s.n_particles
-    out = {"value": n / (ms / 1e3), "unit": "particle-substeps/s (fused G2P2G mode)", "ms_per_substep": ms,
-           "substeps": substeps, "gpu_launches_per_substep": 9,
+    sorts = (substeps + resort - 1) // resort
+    out = {"value": n / (ms_frame / 1e3), "unit": "particle-substeps/s (fused G2P2G mode)",
+           "ms_per_substep": ms_frame, "substeps": substeps, "resort_every": resort,
+           "gpu_launches": sorts * (FINALIZE_LAUNCHES + 4) + (sorts - 1) + (substeps - sorts) * 4 + 1,
+           "ms_per_launch": {k: (sum(v) / len(v) if v else 0.0) for k, v in kt.items()},
+           "per_substep_launches": {"value": n / (ms_sub / 1e3), "ms_per_substep": ms_sub},
            "note": "use_g2p2g=True semantics (reference :363-485): C not stored, p_mass for every material"}
     del s
     torch.cuda.empty_cache()

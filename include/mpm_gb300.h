@@ -194,6 +194,28 @@ int mpm_substep(const MpmParams *p, void *ws, int64_t cap, int64_t n, const floa
 int mpm_frame(const MpmParams *p, void *ws, int64_t cap, int64_t n, float *a, float *b, float dt, int32_t count,
               int32_t resort, float *maxv, int32_t *in_b, void *const *events, void *stream);
 
+/* `count` substeps of the fused G2P2G mode (MPMSolver(use_g2p2g=True)):
+ * engine/mpm_solver.py:773-787 with the g2p2g kernel :363-485, per substep
+ * G2P from the previous substep's grid velocities, advection, the fused
+ * constitutive update and P2G at the new positions, then the grid update
+ * (with the mode's velocity clamp, MpmParams.v_clamp_k).  Every `resort`
+ * substeps (and at the first) the particle kernel reads `a`/`b` in storage
+ * order and writes each particle to its slot sorted by grid block in the
+ * other buffer; in between it runs in place.  The state after the call is
+ * binned (counts) and its bounding box reduced, as after mpm_frame.
+ * Particles with id >= first_new skip the first substep's gather (they keep
+ * their v with C = 0), as particles added since the last substep do in the
+ * reference (last_time_final_particles); first_new = 0 before the first
+ * substep of a solver.  C is not stored in this mode.  Preconditions as for
+ * mpm_frame, plus: the workspace's grid velocities are those of the previous
+ * substep for the particles with id < first_new.  `maxv` receives max |v|
+ * per substep; `events` as for mpm_frame (events[5k+1] after the binning
+ * pass of a sort substep, [5 count] and [5 count + 1] around the frame's
+ * closing binning pass). */
+int mpm_g2p2g_frame(const MpmParams *p, void *ws, int64_t cap, int64_t n, float *a, float *b, float dt,
+                    int32_t count, int32_t resort, int64_t first_new, float *maxv, int32_t *in_b,
+                    void *const *events, void *stream);
+
 /* One substep of the fused G2P2G mode (MPMSolver(use_g2p2g=True),
  * engine/mpm_solver.py:363-485 and :773-787): G2P from the grid velocities of
  * the previous substep, advection, the constitutive update and P2G at the new

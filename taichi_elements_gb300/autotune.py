@@ -53,6 +53,7 @@ def _key(solver, what="chunk") -> str:
     dev = torch.cuda.get_device_name(solver.device)
     bucket = int(math.log2(max(solver.n_particles, 1)))
     key = f"{dev}|{bucket}|{'x'.join(map(str, solver.res))}|{int(solver.per_particle_E)}"
+    key += f"|{'g2p2g' if solver.use_g2p2g else 'plain'}{'|q' if solver.quant else ''}"
     return key if what == "chunk" else f"{what}|{key}|{material_mix(solver)}"
 
 
@@ -95,13 +96,21 @@ def time_chunks(solver, candidates=CANDIDATES, substeps=8, dt=None):
         _lib.check(lib.mpm_bin_count(pp, ws.data_ptr(), cap, bufs[0].data_ptr(), 0, n, stream.cuda_stream),
                    "mpm_bin_count")
         cur = 0
+        calls = 0
 
         def run(k):
-            nonlocal cur
+            nonlocal cur, calls
             for _ in range(k):
-                _lib.check(lib.mpm_substep(pp, ws.data_ptr(), cap, n, bufs[cur].data_ptr(), bufs[1 - cur].data_ptr(),
-                                           dt, None, stream.cuda_stream), "mpm_substep")
+                a, b = bufs[cur].data_ptr(), bufs[1 - cur].data_ptr()
+                if solver.use_g2p2g:  # the first call finalizes the counts and gathers nothing
+                    _lib.check(lib.mpm_g2p2g_substep(pp, ws.data_ptr(), cap, n, a, b, dt, n if calls else 0,
+                                                     0 if calls else 1, None, stream.cuda_stream),
+                               "mpm_g2p2g_substep")
+                else:
+                    _lib.check(lib.mpm_substep(pp, ws.data_ptr(), cap, n, a, b, dt, None, stream.cuda_stream),
+                               "mpm_substep")
                 cur = 1 - cur
+                calls += 1
 
         run(2)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -152,14 +161,21 @@ def time_frames(solver, candidates=RESORT_CANDIDATES, substeps=24, dt=None):
         _lib.check(lib.mpm_bin_count(pp, ws.data_ptr(), cap, bufs[0].data_ptr(), 0, n, stream.cuda_stream),
                    "mpm_bin_count")
         cur = 0
+        frames = 0
 
         def frame():
-            nonlocal cur
+            nonlocal cur, frames
             in_b = ctypes.c_int32(0)
-            _lib.check(lib.mpm_frame(pp, ws.data_ptr(), cap, n, bufs[cur].data_ptr(), bufs[1 - cur].data_ptr(),
-                                     dt, substeps, int(r), maxv.data_ptr(), ctypes.byref(in_b), None,
-                                     stream.cuda_stream), "mpm_frame")
+            a, b = bufs[cur].data_ptr(), bufs[1 - cur].data_ptr()
+            if solver.use_g2p2g:  # the first frame's first substep gathers nothing
+                _lib.check(lib.mpm_g2p2g_frame(pp, ws.data_ptr(), cap, n, a, b, dt, substeps, int(r),
+                                               n if frames else 0, maxv.data_ptr(), ctypes.byref(in_b), None,
+                                               stream.cuda_stream), "mpm_g2p2g_frame")
+            else:
+                _lib.check(lib.mpm_frame(pp, ws.data_ptr(), cap, n, a, b, dt, substeps, int(r), maxv.data_ptr(),
+                                         ctypes.byref(in_b), None, stream.cuda_stream), "mpm_frame")
             cur = (cur + in_b.value) % 2
+            frames += 1
 
         frame()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -184,7 +200,7 @@ def tune_schedule(solver, resort_candidates=RESORT_CANDIDATES, chunk_candidates=
     if best is None:
         chunks = time_chunks(solver, chunk_candidates, substeps=8)
         chunk = min(chunks, key=chunks.get)
-        frames = {} if solver.quant or solver.use_g2p2g else time_frames(solver, resort_candidates, substeps)
+        frames = {} if solver.quant else time_frames(solver, resort_candidates, substeps)
         best = {"chunk": int(chunk), "substep_ms": {str(c): t for c, t in chunks.items()},
                 "frame_ms": {str(r): t for r, t in frames.items()}}
         if frames and min(frames.values()) < chunks[chunk]:

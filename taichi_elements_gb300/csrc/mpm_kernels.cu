@@ -1015,14 +1015,27 @@ __device__ __forceinline__ void fused_stage(FusedWarpSmem &sm, const CUtensorMap
   }
 }
 
-template <bool HAS_EP>
+// Modes of the fused kernel: the plain loop in place (G2P of substep s-1,
+// P2G of substep s), and the G2P2G mode (engine/mpm_solver.py:363-485) in
+// place or writing every state row to the particle's sorted slot inv[i] of
+// another buffer (the substep that re-sorts).
+constexpr int kFusedPlain = 0, kFusedG2P2G = 1, kFusedG2P2GSorted = 2;
+
+template <bool HAS_EP, int MODE>
 __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_fused(const MpmParams P, const Ws w,
                                                                           const __grid_constant__ CUtensorMap map_x,
                                                                           const __grid_constant__ CUtensorMap map_f,
-                                                                          float *__restrict__ st, int64_t cap,
-                                                                          int64_t n, float dt, float *maxv_out) {
+                                                                          float *__restrict__ st,
+                                                                          float *__restrict__ out, int64_t cap,
+                                                                          int64_t n, float dt, int64_t first_new,
+                                                                          float *maxv_out) {
   using R = PRows<false>;
-  constexpr int NF = HAS_EP ? kFusedRowsF : kFusedRowsF - 2;  // F, Jp, material[, id, E]
+  constexpr bool G2P2G = MODE != kFusedPlain;
+  constexpr bool SORTED = MODE == kFusedG2P2GSorted;
+  // staged rows from F on: F, Jp, material[, id][, E].  Only the sorted pass
+  // needs the id: particles added since the last substep (id >= first_new)
+  // exist only at a frame's first substep, which always sorts
+  constexpr int NF = HAS_EP ? kFusedRowsF : (SORTED ? kFusedRowsF - 1 : kFusedRowsF - 2);
   extern __shared__ __align__(128) unsigned char fused_smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   FusedWarpSmem &sm = reinterpret_cast<FusedWarpSmem *>(fused_smem)[warp];
@@ -1056,55 +1069,98 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_fused(const M
     for (int a = 0; a < 9; ++a) F[a / 3][a % 3] = sm.bf[a][lane];
     float Jp = sm.bf[9][lane];
     const int matword = __float_as_int(sm.bf[10][lane]);
+    const int idword = SORTED ? __float_as_int(sm.bf[11][lane]) : 0;
     const float Ep = HAS_EP ? sm.bf[12][lane] : 0.0f;
     __syncwarp();
     const int g1 = step_queue_next(w, kFusedQueue, lane, nsteps, nwarps, q_next, q_end);
     if (g1 >= 0) fused_stage<NF>(sm, map_x, map_f, g1, lane);
     const int64_t i = (int64_t)g0 * 32 + lane;
-    const bool act = i < n;
+    bool act = i < n;
+    int64_t j = i;  // where the particle's state goes
+    if (SORTED && act) {
+      j = w.inv[i];
+      if (j < 0 || j >= n) {  // no sorted slot: the binning was not of this state
+        bad |= MPM_STATUS_TABLE_OVERFLOW;
+        act = false;
+      }
+    }
     const int mat = matword & 0xFF;
     float v[3] = {0.f, 0.f, 0.f}, C[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
     uint32_t bad_b = 0;
     if (act) {
-      // G2P of the previous substep, :694-724
       const Base b0 = particle_base(P, x[0], x[1], x[2], bad_b);
-      // v and C feed this P2G only: the next substep gathers them afresh and
-      // the frame's closing G2P (k_g2p_stream) stores the final ones
-      if (mat != 4) {
-        gather_vc(P, w.grid_vel, b0, v, C);
+      if (!G2P2G) {
+        // G2P of the previous substep, :694-724.  v and C feed this P2G only:
+        // the next substep gathers them afresh and the frame's closing G2P
+        // (k_g2p_stream) stores the final ones
+        if (mat != 4) {
+          gather_vc(P, w.grid_vel, b0, v, C);
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          x[d] = x[d] + dt * v[d];
-          st[(R::X + d) * cap + i] = x[d];
+          for (int d = 0; d < 3; ++d) {
+            x[d] = x[d] + dt * v[d];
+            st[(R::X + d) * cap + i] = x[d];
+          }
+        } else {  // stationary: v, C and x stay
+#pragma unroll
+          for (int d = 0; d < 3; ++d) v[d] = st[(R::V + d) * cap + i];
+#pragma unroll
+          for (int a = 0; a < 9; ++a) C[a / 3][a % 3] = st[(R::C + a) * cap + i];
         }
-      } else {  // stationary: v, C and x stay
+      } else {
+        // G2P from the previous substep's grid, :373-408: particles added
+        // since then keep their v with C = 0; stationary particles gather C
+        // but keep v and x
+        const bool fresh = SORTED && (int64_t)(uint32_t)idword >= first_new;
+        if (!fresh) gather_vc(P, w.grid_vel, b0, v, C);
+        if (mat == 4 || fresh) {
 #pragma unroll
-        for (int d = 0; d < 3; ++d) v[d] = st[(R::V + d) * cap + i];
+          for (int d = 0; d < 3; ++d) v[d] = st[(R::V + d) * cap + i];
+        }
+        if (mat != 4) {
 #pragma unroll
-        for (int a = 0; a < 9; ++a) C[a / 3][a % 3] = st[(R::C + a) * cap + i];
+          for (int d = 0; d < 3; ++d) x[d] = x[d] + dt * v[d];
+          if (!SORTED) {  // in place: x and v (unchanged for a fresh particle) now
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+              st[(R::X + d) * cap + i] = x[d];
+              st[(R::V + d) * cap + i] = v[d];
+            }
+          }
+        }
       }
       vmax = fmaxf(vmax, fmaxf(fabsf(v[0]), fmaxf(fabsf(v[1]), fabsf(v[2]))));
     }
-    // P2G of this substep at the advected x, :487-584
+    // P2G of this substep at the advected x, :487-584 (:410-485)
     Base bs = particle_base(P, x[0], x[1], x[2], bad_b);
     if (act) bad |= bad_b;
     float mass = 0.f, q[3] = {0.f, 0.f, 0.f}, adx[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
     float wt[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
     if (act) {
-      const P2GOut out = constitutive(P, dt, mat, Ep, F, Jp, C);
+      const P2GOut cu = constitutive<G2P2G, false>(P, dt, mat, Ep, F, Jp, C);
+      float *dst = SORTED ? out : st;
 #pragma unroll
-      for (int a = 0; a < 9; ++a) st[(R::F + a) * cap + i] = F[a / 3][a % 3];
-      st[R::Jp * cap + i] = Jp;
+      for (int a = 0; a < 9; ++a) dst[(R::F + a) * cap + j] = F[a / 3][a % 3];
+      dst[R::Jp * cap + j] = Jp;
+      if (SORTED) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          dst[(R::X + d) * cap + j] = x[d];
+          dst[(R::V + d) * cap + j] = v[d];
+        }
+        dst[R::Mat * cap + j] = __int_as_float(matword);
+        dst[R::Id * cap + j] = __int_as_float(idword);
+        if (HAS_EP) dst[R::Ep * cap + j] = Ep;
+      }
       bspline_weights(bs.fx, wt);
-      mass = out.mass;
+      mass = cu.mass;
 #pragma unroll
       for (int d = 0; d < 3; ++d)
-        q[d] = out.mass * v[d] -
-               P.dx * (out.affine[d][0] * bs.fx[0] + out.affine[d][1] * bs.fx[1] + out.affine[d][2] * bs.fx[2]);
+        q[d] = cu.mass * v[d] -
+               P.dx * (cu.affine[d][0] * bs.fx[0] + cu.affine[d][1] * bs.fx[1] + cu.affine[d][2] * bs.fx[2]);
 #pragma unroll
       for (int r = 0; r < 3; ++r)
 #pragma unroll
-        for (int c = 0; c < 3; ++c) adx[r][c] = out.affine[r][c] * P.dx;
+        for (int c = 0; c < 3; ++c) adx[r][c] = cu.affine[r][c] * P.dx;
     }
     p2g_scatter_step<true>(P, w, sm.tile, o, anchored, act, bs, wt, mass, q, adx, lane);
     g0 = g1;
@@ -1117,6 +1173,41 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_fused(const M
     if (lane == 0 && vmax > 0.0f) atomicMax((int *)maxv_out, __float_as_int(vmax));
   }
   step_queue_done(w, kFusedQueue, kFusedDone, lane, nwarps);
+}
+
+// Plain binning of every particle of `st` in storage order (the counts the
+// next sort finalizes) and, when `box` is set, the particles' bounding box.
+__global__ __launch_bounds__(256) void k_bin_box(const MpmParams P, const Ws w, const float *__restrict__ st,
+                                                 int64_t cap, int64_t n, int box) {
+  using R = PRows<false>;
+  uint32_t bad = 0;
+  float bmin[3] = {INFINITY, INFINITY, INFINITY}, bmax[3] = {-INFINITY, -INFINITY, -INFINITY};
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    float x[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      x[d] = st[(R::X + d) * cap + i];
+      bmin[d] = fminf(bmin[d], x[d]);
+      bmax[d] = fmaxf(bmax[d], x[d]);
+    }
+    bin_one<false>(P, nullptr, w, i, x[0], x[1], x[2], 0, bad);
+  }
+  set_status(w, bad);
+  if (box) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        bmin[d] = fminf(bmin[d], __shfl_xor_sync(0xffffffffu, bmin[d], o));
+        bmax[d] = fmaxf(bmax[d], __shfl_xor_sync(0xffffffffu, bmax[d], o));
+      }
+      if ((threadIdx.x & 31) == 0 && bmin[d] <= bmax[d]) {
+        atomicMin(&w.counters[kBoxMin + d], float_key_i32(bmin[d]));
+        atomicMax(&w.counters[kBoxMax + d], float_key_i32(bmax[d]));
+      }
+    }
+  }
 }
 
 // G2P of the last substep of a fused run, in the storage order, with the
@@ -1506,8 +1597,19 @@ struct DevInfo {
   int p2g_ctas = 0, p2g_ep_ctas = 0, g2p_ctas = 0, g2p2g_ctas = 0;
   int p2g_b_ctas = 0, p2g_ep_b_ctas = 0, g2p_b_ctas = 0;
   int p2g_q_ctas = 0, p2g_ep_q_ctas = 0, g2p_q_ctas = 0, g2p2g_q_ctas = 0;  // packed storage
-  int fused_ctas = 0, fused_ep_ctas = 0, g2ps_ctas = 0;  // fused plain substeps
+  int fused_ctas[2][3] = {{0, 0, 0}, {0, 0, 0}};  // k_fused [has_Ep][mode]
+  int g2ps_ctas = 0, binbox_ctas = 0;
 };
+
+// CTAs of one full wave of k_fused<HAS_EP, MODE> (its dynamic shared memory
+// opted in first)
+template <bool HAS_EP, int MODE>
+static void fused_occupancy(int sms, int &ctas) {
+  int k = 0;
+  cudaFuncSetAttribute(k_fused<HAS_EP, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFusedSmem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, k_fused<HAS_EP, MODE>, kP2GThreads, kFusedSmem);
+  ctas = sms * (k > 0 ? k : 1);
+}
 
 static DevInfo g_dev[64];
 static std::mutex g_dev_mu;
@@ -1545,15 +1647,17 @@ static const DevInfo *dev_info() {
     d.p2g_ep_b_ctas = sms * (b2 > 0 ? b2 : 1);
     d.g2p_b_ctas = sms * (c2 > 0 ? c2 : 1);
     {
-      int fa = 0, fb = 0, gs = 0;
-      cudaFuncSetAttribute(k_fused<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFusedSmem);
-      cudaFuncSetAttribute(k_fused<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFusedSmem);
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fa, k_fused<false>, kP2GThreads, kFusedSmem);
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fb, k_fused<true>, kP2GThreads, kFusedSmem);
+      fused_occupancy<false, kFusedPlain>(sms, d.fused_ctas[0][0]);
+      fused_occupancy<true, kFusedPlain>(sms, d.fused_ctas[1][0]);
+      fused_occupancy<false, kFusedG2P2G>(sms, d.fused_ctas[0][1]);
+      fused_occupancy<true, kFusedG2P2G>(sms, d.fused_ctas[1][1]);
+      fused_occupancy<false, kFusedG2P2GSorted>(sms, d.fused_ctas[0][2]);
+      fused_occupancy<true, kFusedG2P2GSorted>(sms, d.fused_ctas[1][2]);
+      int gs = 0, bb = 0;
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&gs, k_g2p_stream, 128, 0);
-      d.fused_ctas = sms * (fa > 0 ? fa : 1);
-      d.fused_ep_ctas = sms * (fb > 0 ? fb : 1);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bb, k_bin_box, 256, 0);
       d.g2ps_ctas = sms * (gs > 0 ? gs : 1);
+      d.binbox_ctas = sms * (bb > 0 ? bb : 1);
     }
     d.sms = sms;
   }
@@ -1764,23 +1868,26 @@ int mpm_substep(const MpmParams *p, void *ws, int64_t cap, int64_t n, const floa
   return mpm_g2p(p, ws, cap, n, nxt, dt, maxv_out, stream);
 }
 
-// One fused substep on `st` in place: G2P of the previous substep and P2G
-// of this one (k_fused), the grid-active list from the flagged blocks, the
-// grid update.
-// The particle kernel of a fused substep: G2P of the previous substep,
-// advection, constitutive update and P2G, in place on `st`.
-static int fused_particles(const DevInfo *di, cudaStream_t s, const MpmParams &p, const Ws &w, float *st, int64_t cap,
-                           int64_t n, float dt, float *maxv) {
+// The particle kernel of a fused substep on `st`: the G2P of the previous
+// substep, advection, the constitutive update and the P2G of this one (MODE:
+// the plain loop in place, or the G2P2G mode in place or into `out` sorted).
+extern "C++" {
+template <int MODE>
+static int fused_particles(const DevInfo *di, cudaStream_t s, const MpmParams &p, const Ws &w, float *st, float *out,
+                           int64_t cap, int64_t n, float dt, int64_t first_new, float *maxv) {
   CUtensorMap mx, mf;
-  const int nf = p.has_Ep ? kFusedRowsF : kFusedRowsF - 2;
+  const int nf = p.has_Ep ? kFusedRowsF : (MODE == kFusedG2P2GSorted ? kFusedRowsF - 1 : kFusedRowsF - 2);
   if (!rows_tensor_map(&mx, st, cap, MPM_NROWS, 3) || !rows_tensor_map(&mf, st, cap, MPM_NROWS, nf))
     return MPM_E_CUDA;
   if (p.has_Ep)
-    k_fused<true><<<di->fused_ep_ctas, kP2GThreads, kFusedSmem, s>>>(p, w, mx, mf, st, cap, n, dt, maxv);
+    k_fused<true, MODE><<<di->fused_ctas[1][MODE], kP2GThreads, kFusedSmem, s>>>(p, w, mx, mf, st, out, cap, n, dt,
+                                                                                  first_new, maxv);
   else
-    k_fused<false><<<di->fused_ctas, kP2GThreads, kFusedSmem, s>>>(p, w, mx, mf, st, cap, n, dt, maxv);
+    k_fused<false, MODE><<<di->fused_ctas[0][MODE], kP2GThreads, kFusedSmem, s>>>(p, w, mx, mf, st, out, cap, n, dt,
+                                                                                   first_new, maxv);
   return MPM_OK;
 }
+}  // extern "C++"
 
 // The grid half of a fused substep: the blocks the particles marked become
 // the grid-active list, then the grid update over them.
@@ -1868,19 +1975,24 @@ int mpm_substep_noalloc(const MpmParams *p, int64_t cap, int64_t n, const float 
   return last_error();
 }
 
-int mpm_frame(const MpmParams *p, void *ws, int64_t cap, int64_t n, float *a, float *b, float dt, int32_t count,
-              int32_t resort, float *maxv, int32_t *in_b, void *const *events, void *stream) {
+// The frame driver of mpm_frame (G2P2G false) and mpm_g2p2g_frame.
+// events[5k + j]: substep k's start, after the binning of the state (a sort
+// substep of the G2P2G mode) or the closing G2P of the previous plain run,
+// after the finalize, after the particle kernel, after the grid update;
+// events[5 count], [5 count + 1] bracket the frame's closing pass.
+extern "C++" {
+template <bool G2P2G>
+static int run_frame(const MpmParams *p, void *ws, int64_t cap, int64_t n, float *a, float *b, float dt,
+                     int32_t count, int32_t resort, int64_t first_new, float *maxv, int32_t *in_b,
+                     void *const *events, void *stream) {
   if (!params_ok(p) || p->quant || p->n_scenes > 0 || !ws || !a || !b || !maxv || !in_b || n < 0 || n > cap ||
-      count < 1 || resort < 1 || !p2g_rows_ok(a, cap) || !p2g_rows_ok(b, cap))
+      count < 1 || resort < 1 || first_new < 0 || !p2g_rows_ok(a, cap) || !p2g_rows_ok(b, cap))
     return MPM_E_INVALID;
   const DevInfo *di = dev_info();
   if (!di) return MPM_E_CUDA;
   Ws w;
   ws_layout(*p, cap, (char *)ws, &w);
   cudaStream_t s = (cudaStream_t)stream;
-  // events[5k + j]: substep k's start, after the closing G2P of the previous
-  // sort run, after the finalize, after the particle kernel, after the grid
-  // update; events[5 count], [5 count + 1] bracket the frame's last G2P
   auto mark = [&](int64_t e) {
     if (events) cudaEventRecord((cudaEvent_t)events[e], s);
   };
@@ -1888,18 +2000,34 @@ int mpm_frame(const MpmParams *p, void *ws, int64_t cap, int64_t n, float *a, fl
   int rc = MPM_OK;
   for (int k = 0; k < count; ++k) {
     mark(5 * k);
-    if (k % resort == 0) {
-      // close the previous substep with the binning of this sort, then sort
-      if (k > 0 && n > 0)
-        k_g2p_stream<<<di->g2ps_ctas, 128, 0, s>>>(*p, w, cur, cap, n, dt, maxv + k - 1);
+    const bool sort = k % resort == 0;
+    if (sort) {
+      // the binning of the state for this sort: the previous plain run's
+      // closing G2P bins as it goes; the G2P2G mode bins in a pass of its own
+      if (k > 0 && n > 0) {
+        if (G2P2G)
+          k_bin_box<<<di->binbox_ctas, 256, 0, s>>>(*p, w, cur, cap, n, 0);
+        else
+          k_g2p_stream<<<di->g2ps_ctas, 128, 0, s>>>(*p, w, cur, cap, n, dt, maxv + k - 1);
+      }
       mark(5 * k + 1);
       rc = mpm_bin_finalize(p, ws, cap, n, stream);
       if (rc) return rc;
       mark(5 * k + 2);
-      rc = launch_p2g_single(di, s, *p, w, cur, oth, cap, n, dt);
-      if (rc) return rc;
-      mark(5 * k + 3);
-      k_grid<false><<<di->sms * 8, 256, 0, s>>>(*p, nullptr, w, dt);
+      if (G2P2G) {
+        if (n > 0) {
+          rc = fused_particles<kFusedG2P2GSorted>(di, s, *p, w, cur, oth, cap, n, dt, k == 0 ? first_new : n,
+                                                  maxv + k);
+          if (rc) return rc;
+        }
+        mark(5 * k + 3);
+        fused_grid(s, di, *p, w, dt);
+      } else {
+        rc = launch_p2g_single(di, s, *p, w, cur, oth, cap, n, dt);
+        if (rc) return rc;
+        mark(5 * k + 3);
+        k_grid<false><<<di->sms * 8, 256, 0, s>>>(*p, nullptr, w, dt);
+      }
       float *t = cur;
       cur = oth;
       oth = t;
@@ -1907,7 +2035,9 @@ int mpm_frame(const MpmParams *p, void *ws, int64_t cap, int64_t n, float *a, fl
       mark(5 * k + 1);
       mark(5 * k + 2);
       if (n > 0) {
-        rc = fused_particles(di, s, *p, w, cur, cap, n, dt, maxv + k - 1);
+        rc = G2P2G ? fused_particles<kFusedG2P2G>(di, s, *p, w, cur, nullptr, cap, n, dt, k == 0 ? first_new : n,
+                                                  maxv + k)
+                   : fused_particles<kFusedPlain>(di, s, *p, w, cur, nullptr, cap, n, dt, 0, maxv + k - 1);
         if (rc) return rc;
       }
       mark(5 * k + 3);
@@ -1916,10 +2046,27 @@ int mpm_frame(const MpmParams *p, void *ws, int64_t cap, int64_t n, float *a, fl
     mark(5 * k + 4);
   }
   mark(5 * (int64_t)count);
-  if (n > 0) k_g2p_stream<<<di->g2ps_ctas, 128, 0, s>>>(*p, w, cur, cap, n, dt, maxv + count - 1);
+  if (n > 0) {
+    if (G2P2G)
+      k_bin_box<<<di->binbox_ctas, 256, 0, s>>>(*p, w, cur, cap, n, 1);
+    else
+      k_g2p_stream<<<di->g2ps_ctas, 128, 0, s>>>(*p, w, cur, cap, n, dt, maxv + count - 1);
+  }
   mark(5 * (int64_t)count + 1);
   *in_b = cur == b;
   return last_error();
+}
+}  // extern "C++"
+
+int mpm_frame(const MpmParams *p, void *ws, int64_t cap, int64_t n, float *a, float *b, float dt, int32_t count,
+              int32_t resort, float *maxv, int32_t *in_b, void *const *events, void *stream) {
+  return run_frame<false>(p, ws, cap, n, a, b, dt, count, resort, 0, maxv, in_b, events, stream);
+}
+
+int mpm_g2p2g_frame(const MpmParams *p, void *ws, int64_t cap, int64_t n, float *a, float *b, float dt,
+                    int32_t count, int32_t resort, int64_t first_new, float *maxv, int32_t *in_b,
+                    void *const *events, void *stream) {
+  return run_frame<true>(p, ws, cap, n, a, b, dt, count, resort, first_new, maxv, in_b, events, stream);
 }
 
 int mpm_max_grid_velocity(const MpmParams *p, void *ws, int64_t cap, float *out, void *stream) {

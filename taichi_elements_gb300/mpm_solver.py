@@ -745,20 +745,38 @@ class MPMSolver:
 
     @property
     def _fuses_frames(self) -> bool:
-        """Frames of the plain substep run as fused substeps (mpm_frame):
-        float32 storage and the reference's plain loop (not use_g2p2g)."""
-        return self.fuse_frames and not self.quant and not self.use_g2p2g
+        """Frames run as fused substeps (mpm_frame for the reference's plain
+        loop, mpm_g2p2g_frame for use_g2p2g): float32 storage only."""
+        return self.fuse_frames and not self.quant
 
     def _launch_frame(self, count: int, dt: float):
-        """All substeps of a frame: the plain loop fused (G2P of one substep
-        with P2G of the next), re-sorted every `resort_every` substeps."""
+        """All substeps of a frame, re-sorted every `resort_every` substeps:
+        the plain loop fused (G2P of one substep with P2G of the next), or
+        the G2P2G mode's substeps."""
         p = self.params
         in_b = ctypes.c_int32(0)
-        _lib.check(
-            self._lib.mpm_frame(ctypes.byref(p), _ptr(self._ws), self._cap, self.n_particles,
-                                _ptr(self._state[self._cur]), _ptr(self._state[1 - self._cur]), float(dt), int(count),
-                                int(self.resort_every), _ptr(self._maxv), ctypes.byref(in_b), None, self.stream),
-            "mpm_frame")
+        if self.use_g2p2g:
+            if self._g2p2g_listed:  # per-substep calls left finalized lists: count afresh
+                _lib.check(self._lib.mpm_bin_count(ctypes.byref(p), _ptr(self._ws), self._cap,
+                                                   _ptr(self._state[self._cur]), 0, self.n_particles, self.stream),
+                           "mpm_bin_count")
+            first_new = self._last_final if self._g2p2g_grid_valid else 0
+            _lib.check(
+                self._lib.mpm_g2p2g_frame(ctypes.byref(p), _ptr(self._ws), self._cap, self.n_particles,
+                                          _ptr(self._state[self._cur]), _ptr(self._state[1 - self._cur]), float(dt),
+                                          int(count), int(self.resort_every), int(first_new), _ptr(self._maxv),
+                                          ctypes.byref(in_b), None, self.stream), "mpm_g2p2g_frame")
+            # the state is binned (counts) for the next frame or substep
+            self._g2p2g_listed = 0
+            self._binned = self.n_particles
+            self._last_final = self.n_particles
+            self._g2p2g_grid_valid = True
+        else:
+            _lib.check(
+                self._lib.mpm_frame(ctypes.byref(p), _ptr(self._ws), self._cap, self.n_particles,
+                                    _ptr(self._state[self._cur]), _ptr(self._state[1 - self._cur]), float(dt),
+                                    int(count), int(self.resort_every), _ptr(self._maxv), ctypes.byref(in_b), None,
+                                    self.stream), "mpm_frame")
         self._cur = (self._cur + int(in_b.value)) % 2
 
     def _frame_swaps(self, count: int) -> int:
@@ -821,7 +839,7 @@ class MPMSolver:
                 self._check_status()
         elif self.n_particles > 0:
             self._run_frame(count, dt)
-            if self.use_g2p2g:  # the fused kernel does not reduce the bounding box
+            if self.use_g2p2g and not self._fuses_frames:  # k_g2p2g reduces no bounding box
                 maxv = self._maxv[:count].cpu().numpy()
                 self._check_status()
                 self._host_box = None

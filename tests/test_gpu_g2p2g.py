@@ -137,3 +137,73 @@ def test_g2p2g_grid_velocity_clamp(v_clamp):
         assert np.all(vmax <= va * (1 + 1e-6)), vmax
     else:
         assert vmax[0] > 1.3 * va, vmax
+
+
+@pytest.mark.parametrize("resort", [1, 3, 16])
+def test_g2p2g_frames_match_oracle(resort):
+    """step() frames of the mode through mpm_g2p2g_frame: re-sorted every
+    `resort` substeps (1: every substep writes the sorted order), in place in
+    between."""
+    sc = scenes.four_materials_128(per_cube=8000)
+    s, R64, R32, win = start(sc)
+    s.resort_every = resort
+    count, dt = s.count_substeps(20 * sc.default_dt * 0.999, sc.default_dt)
+    s.step(20 * sc.default_dt * 0.999)
+    assert s.total_substeps == count
+    for _ in range(count):
+        R64.step(dt)
+        R32.step(dt)
+    assert_bounds(f"{sc.name} G2P2G frame of {count} substeps, re-sort every {resort}", errors(s, R64, R32, win),
+                  f32_calibrated=True)
+
+
+def test_g2p2g_frames_alternate_with_single_substeps():
+    """A frame, single substeps (the per-substep kernel, as the adaptive-dt
+    loop runs it), then another frame: each hands the binning and the grid to
+    the next."""
+    sc = scenes.smoke_scene()
+    s, R64, R32, win = start(sc)
+    s.resort_every = 4
+    dt = sc.default_dt
+    for kind in ("frame", "substep", "substep", "frame"):
+        if kind == "frame":
+            count, fdt = s.count_substeps(6 * dt * 0.999, dt)
+            s.step(6 * dt * 0.999)
+        else:
+            count, fdt = 1, dt
+            s.substep(dt)
+        for _ in range(count):
+            R64.step(fdt)
+            R32.step(fdt)
+    assert_bounds("smoke G2P2G frames and substeps", errors(s, R64, R32, win), f32_calibrated=True)
+
+
+def test_g2p2g_frame_after_particles_were_added():
+    """Particles added between frames: the next frame's first substep lets
+    them skip the gather (id >= first_new), in the sorted pass."""
+    sc = scenes.smoke_scene()
+    s = sc.make_solver(use_g2p2g=True)
+    s.resort_every = 3
+    for _ in range(2):
+        s.step(1e-3)
+    s.add_cube((0.4, 0.6, 0.4), (0.1, 0.1, 0.1), s.material_water, velocity=(0.0, -1.0, 0.0))
+    cfg = oracle_config(s)
+    st = s.full_state()
+    P = O.Particles(*(st[k].cpu().numpy().astype(np.float64) for k in ('x', 'v', 'C', 'F', 'Jp')),
+                    st['material'].cpu().numpy().astype(np.int32))
+    win = O.Window.covering(P.x, cfg.inv_dx, margin=16)
+    R = O.G2P2GRunner(cfg, P, win)
+    coords, vel = gpu_grid(s.views(), 'grid_vel')
+    gv = np.zeros(tuple(win.W) + (3,))
+    inside = np.all((coords >= win.lo) & (coords < win.lo + win.W), 1)
+    gv[tuple((coords[inside] - win.lo).T)] = vel[inside, :3]
+    R.gv = gv.reshape(-1)
+    R.last_final = s._last_final
+    assert R.last_final < P.n
+    count, dt = s.count_substeps(4 * s.default_dt * 0.999, s.default_dt)
+    s.step(4 * s.default_dt * 0.999)
+    for _ in range(count):
+        R.step(dt)
+    g = gpu_particles(s)
+    assert rel_inf(g['x'], R.P.x, 1.0) < 1e-5
+    assert rel_inf(g['v'], R.P.v, max(np.abs(R.P.v).max(), 1e-3)) < 1e-4

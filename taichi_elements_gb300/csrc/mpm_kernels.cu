@@ -411,10 +411,10 @@ __global__ __launch_bounds__(256) void k_cell_clear(const MpmParams P, const Ws 
 // P2G visits the particles in the order of the state buffer `cur` (the
 // sorted order of the previous substep), 32 consecutive slots per warp step,
 // so each state row of a step is one contiguous 128-byte segment.  Each warp
-// runs its own two-stage pipeline: one lane issues bulk copies (TMA) of the
-// next step's rows and of their sorted slots (`inv`) into one of two shared
-// buffers while the warp works on the current step, so the row loads never
-// stall the warp.  Per particle: constitutive update (engine/mpm_solver.py
+// runs its own two-stage pipeline: once the current step's rows are in
+// registers, one lane issues the bulk copies (TMA) of the next step's rows
+// and of their sorted slots (`inv`) into the warp's staging buffer, which
+// land while the warp works on the current step.  Per particle: constitutive update (engine/mpm_solver.py
 // :506-574), the updated state written to its sorted slot `inv[i]` of `nxt`,
 // and the APIC scatter (:576-584) into the warp's 8^3 float4 tile of grid
 // nodes with plain shared-memory read-modify-writes.  The tile is anchored at

@@ -261,28 +261,28 @@ def time_frames(solver, dt, plan, stream):
             if solver.use_g2p2g:  # every particle took part in the previous substep
                 _lib.check(solver._lib.mpm_g2p2g_frame(ctypes.byref(p), solver._ws.data_ptr(), solver._cap,
                                                        solver.n_particles, a, b, float(dt), int(c),
-                                                       int(solver.resort_every), solver.n_particles,
+                                                       solver._frame_resort(c), solver.n_particles,
                                                        solver._maxv.data_ptr(), ctypes.byref(in_b), arr,
                                                        stream.cuda_stream), "mpm_g2p2g_frame")
             else:
                 _lib.check(solver._lib.mpm_frame(ctypes.byref(p), solver._ws.data_ptr(), solver._cap,
                                                  solver.n_particles, a, b, float(dt), int(c),
-                                                 int(solver.resort_every), solver._maxv.data_ptr(),
+                                                 solver._frame_resort(c), solver._maxv.data_ptr(),
                                                  ctypes.byref(in_b), arr, stream.cuda_stream), "mpm_frame")
             solver._cur = (solver._cur + in_b.value) % 2
     return evs, run
 
 
-def frame_kernel_times(plan, evs, resort, g2p2g=False):
+def frame_kernel_times(plan, evs, resorts, g2p2g=False):
     """Per launch group durations (ms) from the events of time_frames.  Plain
     frames: the sort's P2G (k_p2g), the fused substeps (k_fused), the closing
     G2P that also bins (k_g2p_stream); G2P2G frames: the sorting pass
     (k_fused_sorted), the in-place substeps (k_fused) and the binning passes
     (k_bin_box).  "binning" is the sorts' finalize, "grid" the grid update
-    with the flag passes."""
+    with the flag passes.  `resorts`: each frame's re-sort interval."""
     sort_k, bin_k = ("k_fused_sorted", "k_bin_box") if g2p2g else ("k_p2g", "k_g2p_stream")
     out = {sort_k: [], "k_fused": [], bin_k: [], "binning": [], "grid": []}
-    for c, ev in zip(plan, evs):
+    for c, ev, resort in zip(plan, evs, resorts):
         def t(i, j):
             return ev[i].elapsed_time(ev[j])
         for k in range(c):
@@ -384,8 +384,9 @@ def run_gb300(args):
     sub_bytes = (Q_ALGO_BYTES_PER_PARTICLE if args.quant else ALGO_BYTES_PER_PARTICLE) * n + \
         ALGO_BYTES_PER_NODE * n_nodes
     if fused:
-        kt = frame_kernel_times(plan, evs, solver.resort_every)
-        launches = sum(frame_launches(c, solver.resort_every) for c in plan)
+        resorts = [solver._frame_resort(c) for c in plan]
+        kt = frame_kernel_times(plan, evs, resorts)
+        launches = sum(frame_launches(c, r) for c, r in zip(plan, resorts))
         totals = {k: float(sum(v)) for k, v in kt.items()}
         phases = {k: totals[k] / args.steps for k in totals}
         per_launch = {k: (totals[k] / len(v) if v else 0.0) for k, v in kt.items()}
@@ -394,6 +395,7 @@ def run_gb300(args):
                         "k_g2p_stream": G2P_BYTES_PER_PARTICLE * n + G2P_BYTES_PER_NODE * n_nodes}
         top = max(kernel_bytes, key=lambda k: totals[k])
         schedule = {"mode": "fused frames (mpm_frame)", "resort_every": solver.resort_every,
+                    "resort_per_frame": resorts,
                     "frames": plan, "launches_per_kernel": {k: len(v) for k, v in kt.items()},
                     "ms_per_launch": per_launch}
     else:
@@ -732,7 +734,7 @@ def run_g2p2g_measure(sc, resort, substeps=50, warmup=5):
     s._launch_substeps(warmup, dt)  # the first frame: fresh particles, the mode's state
     evs, run = time_frames(s, dt, [substeps], stream)
     ms_frame = timed(run)
-    kt = frame_kernel_times([substeps], evs, resort, g2p2g=True)
+    kt = frame_kernel_times([substeps], evs, [s._frame_resort(substeps)], g2p2g=True)
     s.fuse_frames = False
     s._g2p2g_listed = 0  # time_frames left the state binned (counts), as a frame does
     for _ in range(warmup):
@@ -741,7 +743,8 @@ def run_g2p2g_measure(sc, resort, substeps=50, warmup=5):
     if int(s._status.item()):
         raise RuntimeError("device status set during the G2P2G measurement")
     n = s.n_particles
-    sorts = (substeps + resort - 1) // resort
+    eff = s._frame_resort(substeps)
+    sorts = (substeps + eff - 1) // eff
     out = {"value": n / (ms_frame / 1e3), "unit": "particle-substeps/s (fused G2P2G mode)",
            "ms_per_substep": ms_frame, "substeps": substeps, "resort_every": resort,
            "gpu_launches": sorts * (FINALIZE_LAUNCHES + 4) + (sorts - 1) + (substeps - sorts) * 4 + 1,

@@ -8,10 +8,11 @@ arithmetic:
   The engine splits each active 4^3 grid block's particles into work items of
   `chunk` particles; large items amortise the halo staging, small items give
   a small scene enough CTAs to fill 152 SMs.
-* fused frames (mpm_frame): the particles are re-sorted every `resort`
-  substeps; in between, the G2P of one substep (velocity gathers through L1,
-  no halo staging) and the P2G of the next run as one kernel.  Frequent sorts
-  keep the scatter tiles dense; rare sorts save the sort's data movement.
+* fused frames (mpm_frame): the particles are re-sorted about every
+  `resort` substeps (evenly over the frame); in between, the G2P of one
+  substep (velocity gathers through L1, no halo staging) and the P2G of the
+  next run as one kernel.  Frequent sorts keep the scatter tiles dense; rare
+  sorts save the sort's data movement.
 
 ``tune_chunk`` times the chunk candidates; ``tune_schedule`` times fused
 frames for each re-sort candidate against the per-substep schedule at its
@@ -34,7 +35,7 @@ import torch
 from . import _lib
 
 CANDIDATES = (128, 256, 512, 1024)
-RESORT_CANDIDATES = (2, 4, 8, 16)
+RESORT_CANDIDATES = (8, 12, 16, 24, 48)
 _cache: dict = {}
 _lock = threading.Lock()
 
@@ -141,9 +142,11 @@ def tune_chunk(solver, candidates=CANDIDATES, substeps=8) -> int:
     return int(best)
 
 
-def time_frames(solver, candidates=RESORT_CANDIDATES, substeps=24, dt=None):
+def time_frames(solver, candidates=RESORT_CANDIDATES, substeps=48, dt=None):
     """Milliseconds per substep of a fused frame of `substeps` substeps for
-    each re-sort interval, measured on a copy."""
+    each target re-sort interval (spread over the frame as step() spreads
+    it), measured on a copy."""
+    from .mpm_solver import frame_resort_interval
     solver._prepare(dt or solver.default_dt)
     dt = float(dt or solver.default_dt)
     lib = solver._lib
@@ -163,16 +166,18 @@ def time_frames(solver, candidates=RESORT_CANDIDATES, substeps=24, dt=None):
         cur = 0
         frames = 0
 
+        eff = frame_resort_interval(substeps, r)
+
         def frame():
             nonlocal cur, frames
             in_b = ctypes.c_int32(0)
             a, b = bufs[cur].data_ptr(), bufs[1 - cur].data_ptr()
             if solver.use_g2p2g:  # the first frame's first substep gathers nothing
-                _lib.check(lib.mpm_g2p2g_frame(pp, ws.data_ptr(), cap, n, a, b, dt, substeps, int(r),
+                _lib.check(lib.mpm_g2p2g_frame(pp, ws.data_ptr(), cap, n, a, b, dt, substeps, eff,
                                                n if frames else 0, maxv.data_ptr(), ctypes.byref(in_b), None,
                                                stream.cuda_stream), "mpm_g2p2g_frame")
             else:
-                _lib.check(lib.mpm_frame(pp, ws.data_ptr(), cap, n, a, b, dt, substeps, int(r), maxv.data_ptr(),
+                _lib.check(lib.mpm_frame(pp, ws.data_ptr(), cap, n, a, b, dt, substeps, eff, maxv.data_ptr(),
                                          ctypes.byref(in_b), None, stream.cuda_stream), "mpm_frame")
             cur = (cur + in_b.value) % 2
             frames += 1
@@ -187,7 +192,7 @@ def time_frames(solver, candidates=RESORT_CANDIDATES, substeps=24, dt=None):
     return out
 
 
-def tune_schedule(solver, resort_candidates=RESORT_CANDIDATES, chunk_candidates=CANDIDATES, substeps=24) -> dict:
+def tune_schedule(solver, resort_candidates=RESORT_CANDIDATES, chunk_candidates=CANDIDATES, substeps=48) -> dict:
     """Measure fused frames for each re-sort interval and per-substep
     launches for each chunk, apply the fastest (solver.fuse_frames,
     solver.resort_every, solver.chunk) and return the choice with the

@@ -64,6 +64,14 @@ class ParticleCount(int):
         raise TypeError("n_particles is a scalar: index it with [None]")
 
 
+def frame_resort_interval(count: int, target: int) -> int:
+    """Re-sort interval for a fused frame of `count` substeps and a target
+    interval: round(count / target) sorts (at least one) at equal spacing,
+    so that no sort serves only the last substep or two of a frame."""
+    sorts = max(1, int(count / max(1, target) + 0.5))
+    return max(1, -(-count // sorts))
+
+
 class MPMSolver:
     material_water = 0
     material_elastic = 1
@@ -174,7 +182,7 @@ class MPMSolver:
         # every `resort_every` substeps (the storage order drifts from the
         # positions in between); autotune.tune_schedule measures both choices
         self.fuse_frames = True
-        self.resort_every = 8
+        self.resort_every = 24
         self.chunk = int(chunk) if chunk else self.DEFAULT_CHUNK
         self.use_cuda_graph = use_cuda_graph
         self.autotune = bool(autotune)
@@ -764,8 +772,8 @@ class MPMSolver:
             _lib.check(
                 self._lib.mpm_g2p2g_frame(ctypes.byref(p), _ptr(self._ws), self._cap, self.n_particles,
                                           _ptr(self._state[self._cur]), _ptr(self._state[1 - self._cur]), float(dt),
-                                          int(count), int(self.resort_every), int(first_new), _ptr(self._maxv),
-                                          ctypes.byref(in_b), None, self.stream), "mpm_g2p2g_frame")
+                                          int(count), int(self._frame_resort(count)), int(first_new),
+                                          _ptr(self._maxv), ctypes.byref(in_b), None, self.stream), "mpm_g2p2g_frame")
             # the state is binned (counts) for the next frame or substep
             self._g2p2g_listed = 0
             self._binned = self.n_particles
@@ -775,13 +783,20 @@ class MPMSolver:
             _lib.check(
                 self._lib.mpm_frame(ctypes.byref(p), _ptr(self._ws), self._cap, self.n_particles,
                                     _ptr(self._state[self._cur]), _ptr(self._state[1 - self._cur]), float(dt),
-                                    int(count), int(self.resort_every), _ptr(self._maxv), ctypes.byref(in_b), None,
+                                    int(count), int(self._frame_resort(count)), _ptr(self._maxv), ctypes.byref(in_b), None,
                                     self.stream), "mpm_frame")
         self._cur = (self._cur + int(in_b.value)) % 2
 
+    def _frame_resort(self, count: int) -> int:
+        """The re-sort interval of a fused frame of `count` substeps: the
+        number of sorts closest to count / resort_every (at least one),
+        spread evenly over the frame."""
+        return frame_resort_interval(count, self.resort_every)
+
     def _frame_swaps(self, count: int) -> int:
         """Buffer swaps of a fused frame: one per sort."""
-        return (count + self.resort_every - 1) // self.resort_every
+        r = self._frame_resort(count)
+        return (count + r - 1) // r
 
     def _launch_substeps(self, count: int, dt: float):
         self._maxv[:count].zero_()

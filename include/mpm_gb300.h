@@ -246,6 +246,19 @@ int mpm_batch_bin_count(const MpmParams *p, const MpmParams *scenes, void *ws, i
 int mpm_batch_substep(const MpmParams *p, const MpmParams *scenes, void *ws, int64_t cap, int64_t n,
                       const float *cur, float *nxt, float *maxv_out, void *stream);
 
+/* Batched frame: `count` substeps of every scene of the batch (each at its
+ * own MpmParams.dt), as mpm_frame does for one scene: re-sorted every
+ * `resort` substeps (and at the first), the G2P of one substep fused with
+ * the P2G of the next in between.  Preconditions as for mpm_batch_substep
+ * (the workspace holds the binning counts of the state in `a`) and
+ * mpm_frame's buffer rules.  `maxv` receives n_scenes floats per substep
+ * (the scenes' max |v|); on return `*in_b` is 1 when the state ends in `b`.
+ * `events` as for mpm_frame.  No counterpart in the reference, which runs
+ * one MPMSolver per scene. */
+int mpm_batch_frame(const MpmParams *p, const MpmParams *scenes, void *ws, int64_t cap, int64_t n, float *a,
+                    float *b, int32_t count, int32_t resort, float *maxv, int32_t *in_b, void *const *events,
+                    void *stream);
+
 /* ---- Adjoint of one substep (water and elastic) ----------------------
  * No counterpart in the reference, which has no autodiff.  Gradient buffers
  * `gin` / `gout` have 26 float32 rows of `cap` columns: dL/dx (rows 0-2),

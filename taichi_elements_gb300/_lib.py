@@ -110,6 +110,7 @@ SIGNATURES = {
     "mpm_substep": [_P, _v, _i64, _i64, _v, _v, _f, _v, _v],
     "mpm_frame": [_P, _v, _i64, _i64, _v, _v, _f, _i32, _i32, _v, _v, _v, _v],
     "mpm_g2p2g_frame": [_P, _v, _i64, _i64, _v, _v, _f, _i32, _i32, _i64, _v, _v, _v, _v],
+    "mpm_batch_frame": [_P, _v, _v, _i64, _i64, _v, _v, _i32, _i32, _v, _v, _v, _v],
     "mpm_g2p2g_substep": [_P, _v, _i64, _i64, _v, _v, _f, _i64, _i32, _v, _v],
     "mpm_substep_noalloc": [_P, _i64, _i64, _v, _v, _f, _v, _v],
     "mpm_batch_bin_count": [_P, _v, _v, _i64, _v, _i64, _i64, _v],

@@ -951,8 +951,8 @@ __device__ __forceinline__ void stencil_addresses(const MpmParams &P, const int 
 }
 
 // G2P gather (:711-721) straight from the grid velocities: v and C.
-__device__ __forceinline__ void gather_vc(const MpmParams &P, const float4 *__restrict__ gv, const Base &b,
-                                          float (&nv)[3], float (&nC)[3][3]) {
+__device__ __forceinline__ void gather_vc(const MpmParams &P, float inv_dx, const float4 *__restrict__ gv,
+                                          const Base &b, float (&nv)[3], float (&nC)[3][3]) {
   float wt[3][3];
   bspline_weights(b.fx, wt);
   int ax[3], ay[3], az[3];
@@ -981,7 +981,7 @@ __device__ __forceinline__ void gather_vc(const MpmParams &P, const float4 *__re
         if (bb > 0) sb[r] = fmaf((float)bb * W, T[r], sb[r]);
       }
     }
-  const float s4 = 4.0f * P.inv_dx;
+  const float s4 = 4.0f * inv_dx;
 #pragma unroll
   for (int r = 0; r < 3; ++r) {
     nC[r][0] = s4 * fmaf(-nv[r], b.fx[0], sa[r]);
@@ -1015,14 +1015,34 @@ __device__ __forceinline__ void fused_stage(FusedWarpSmem &sm, const CUtensorMap
   }
 }
 
+// Scene index in the material word of a batched particle (bits 8..30).
+__device__ __forceinline__ int scene_index_of_particle(const MpmParams &P, int matword) {
+  return min(max(matword >> 8, 0), P.n_scenes - 1);
+}
+
+// The max |v| of a warp's particles into maxv_out: one slot, or in batched
+// mode the slot of the scene each lane's maximum belongs to.
+template <bool BATCH>
+__device__ __forceinline__ void flush_vmax(float *maxv_out, float vmax, int vscene, int lane) {
+  if (!maxv_out) return;
+  if (BATCH) {
+    if (vmax > 0.0f) atomicMax((int *)&maxv_out[vscene], __float_as_int(vmax));
+    return;
+  }
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, d));
+  if (lane == 0 && vmax > 0.0f) atomicMax((int *)maxv_out, __float_as_int(vmax));
+}
+
 // Modes of the fused kernel: the plain loop in place (G2P of substep s-1,
 // P2G of substep s), and the G2P2G mode (engine/mpm_solver.py:363-485) in
 // place or writing every state row to the particle's sorted slot inv[i] of
 // another buffer (the substep that re-sorts).
 constexpr int kFusedPlain = 0, kFusedG2P2G = 1, kFusedG2P2GSorted = 2;
 
-template <bool HAS_EP, int MODE>
-__global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_fused(const MpmParams P, const Ws w,
+template <bool HAS_EP, int MODE, bool BATCH = false>
+__global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_fused(const MpmParams P, const MpmParams *tab,
+                                                                          const Ws w,
                                                                           const __grid_constant__ CUtensorMap map_x,
                                                                           const __grid_constant__ CUtensorMap map_f,
                                                                           float *__restrict__ st,
@@ -1032,6 +1052,7 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_fused(const M
   using R = PRows<false>;
   constexpr bool G2P2G = MODE != kFusedPlain;
   constexpr bool SORTED = MODE == kFusedG2P2GSorted;
+  static_assert(!(BATCH && G2P2G), "the batched form runs the plain loop");
   // staged rows from F on: F, Jp, material[, id][, E].  Only the sorted pass
   // needs the id: particles added since the last substep (id >= first_new)
   // exist only at a frame's first substep, which always sorts
@@ -1043,6 +1064,7 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_fused(const M
   const int nwarps = (int)gridDim.x * kP2GWarps;
   uint32_t bad = 0;
   float vmax = 0.0f;
+  int vscene = 0;  // batched: the scene vmax belongs to (per lane)
   for (int t = lane; t < kP2GTileN + 1; t += 32) sm.tile[t] = make_float4(0.f, 0.f, 0.f, 0.f);
   if (lane == 0) {
     mbar_init(&sm.bar, 1);
@@ -1085,19 +1107,21 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_fused(const M
       }
     }
     const int mat = matword & 0xFF;
+    const MpmParams &S = scene_of_particle<BATCH>(P, tab, matword);
+    const float dts = BATCH ? S.dt : dt;
     float v[3] = {0.f, 0.f, 0.f}, C[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
     uint32_t bad_b = 0;
     if (act) {
-      const Base b0 = particle_base(P, x[0], x[1], x[2], bad_b);
+      const Base b0 = particle_base(S, x[0], x[1], x[2], bad_b);
       if (!G2P2G) {
         // G2P of the previous substep, :694-724.  v and C feed this P2G only:
         // the next substep gathers them afresh and the frame's closing G2P
         // (k_g2p_stream) stores the final ones
         if (mat != 4) {
-          gather_vc(P, w.grid_vel, b0, v, C);
+          gather_vc(P, S.inv_dx, w.grid_vel, b0, v, C);
 #pragma unroll
           for (int d = 0; d < 3; ++d) {
-            x[d] = x[d] + dt * v[d];
+            x[d] = x[d] + dts * v[d];
             st[(R::X + d) * cap + i] = x[d];
           }
         } else {  // stationary: v, C and x stay
@@ -1111,7 +1135,7 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_fused(const M
         // since then keep their v with C = 0; stationary particles gather C
         // but keep v and x
         const bool fresh = SORTED && (int64_t)(uint32_t)idword >= first_new;
-        if (!fresh) gather_vc(P, w.grid_vel, b0, v, C);
+        if (!fresh) gather_vc(P, S.inv_dx, w.grid_vel, b0, v, C);
         if (mat == 4 || fresh) {
 #pragma unroll
           for (int d = 0; d < 3; ++d) v[d] = st[(R::V + d) * cap + i];
@@ -1128,15 +1152,24 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_fused(const M
           }
         }
       }
-      vmax = fmaxf(vmax, fmaxf(fabsf(v[0]), fmaxf(fabsf(v[1]), fabsf(v[2]))));
+      const float vm = fmaxf(fabsf(v[0]), fmaxf(fabsf(v[1]), fabsf(v[2])));
+      if (BATCH) {
+        const int sc = scene_index_of_particle(P, matword);
+        if (sc != vscene) {  // per-scene maxima: flush when this lane's scene changes
+          if (maxv_out && vmax > 0.0f) atomicMax((int *)&maxv_out[vscene], __float_as_int(vmax));
+          vmax = 0.0f;
+          vscene = sc;
+        }
+      }
+      vmax = fmaxf(vmax, vm);
     }
     // P2G of this substep at the advected x, :487-584 (:410-485)
-    Base bs = particle_base(P, x[0], x[1], x[2], bad_b);
+    Base bs = particle_base(S, x[0], x[1], x[2], bad_b);
     if (act) bad |= bad_b;
     float mass = 0.f, q[3] = {0.f, 0.f, 0.f}, adx[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
     float wt[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
     if (act) {
-      const P2GOut cu = constitutive<G2P2G, false>(P, dt, mat, Ep, F, Jp, C);
+      const P2GOut cu = constitutive<G2P2G, false>(S, dts, mat, Ep, F, Jp, C);
       float *dst = SORTED ? out : st;
 #pragma unroll
       for (int a = 0; a < 9; ++a) dst[(R::F + a) * cap + j] = F[a / 3][a % 3];
@@ -1156,22 +1189,18 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_fused(const M
 #pragma unroll
       for (int d = 0; d < 3; ++d)
         q[d] = cu.mass * v[d] -
-               P.dx * (cu.affine[d][0] * bs.fx[0] + cu.affine[d][1] * bs.fx[1] + cu.affine[d][2] * bs.fx[2]);
+               S.dx * (cu.affine[d][0] * bs.fx[0] + cu.affine[d][1] * bs.fx[1] + cu.affine[d][2] * bs.fx[2]);
 #pragma unroll
       for (int r = 0; r < 3; ++r)
 #pragma unroll
-        for (int c = 0; c < 3; ++c) adx[r][c] = cu.affine[r][c] * P.dx;
+        for (int c = 0; c < 3; ++c) adx[r][c] = cu.affine[r][c] * S.dx;
     }
     p2g_scatter_step<true>(P, w, sm.tile, o, anchored, act, bs, wt, mass, q, adx, lane);
     g0 = g1;
   }
   if (anchored) p2g_tile_flush<true>(P, w, sm.tile, o, lane);
   set_status(w, bad);
-  if (maxv_out) {
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, d));
-    if (lane == 0 && vmax > 0.0f) atomicMax((int *)maxv_out, __float_as_int(vmax));
-  }
+  flush_vmax<BATCH>(maxv_out, vmax, vscene, lane);
   step_queue_done(w, kFusedQueue, kFusedDone, lane, nwarps);
 }
 
@@ -1214,14 +1243,17 @@ __global__ __launch_bounds__(256) void k_bin_box(const MpmParams P, const Ws w, 
 // plain binning for the next sort (in-cell ranks from arrival order: the
 // storage order no longer matches the last sort's ranks), the max |v| and
 // the particles' bounding box.
-__global__ __launch_bounds__(128, 5) void k_g2p_stream(const MpmParams P, const Ws w, float *__restrict__ st,
-                                                      int64_t cap, int64_t n, float dt, float *maxv_out) {
+template <bool BATCH>
+__global__ __launch_bounds__(128, 5) void k_g2p_stream(const MpmParams P, const MpmParams *tab, const Ws w,
+                                                      float *__restrict__ st, int64_t cap, int64_t n, float dt,
+                                                      float *maxv_out) {
   using R = PRows<false>;
   const int lane = threadIdx.x & 31;
   const int nsteps = (int)((n + 31) / 32);
   const int nwarps = (int)gridDim.x * (blockDim.x >> 5);
   uint32_t bad = 0;
   float vmax = 0.0f;
+  int vscene = 0;
   float bmin[3] = {INFINITY, INFINITY, INFINITY}, bmax[3] = {-INFINITY, -INFINITY, -INFINITY};
   int q_next = 0, q_end = 0;
   for (int g = step_queue_next(w, kFusedQueue, lane, nsteps, nwarps, q_next, q_end); g >= 0;
@@ -1232,15 +1264,17 @@ __global__ __launch_bounds__(128, 5) void k_g2p_stream(const MpmParams P, const 
 #pragma unroll
     for (int d = 0; d < 3; ++d) x[d] = st[(R::X + d) * cap + j];
     const int matword = __float_as_int(st[R::Mat * cap + j]);
-    const Base b = particle_base(P, x[0], x[1], x[2], bad);
+    const MpmParams &S = scene_of_particle<BATCH>(P, tab, matword);
+    const Base b = particle_base(S, x[0], x[1], x[2], bad);
     float vv[3];
     if ((matword & 0xFF) != 4) {
       float nC[3][3];
-      gather_vc(P, w.grid_vel, b, vv, nC);
+      gather_vc(P, S.inv_dx, w.grid_vel, b, vv, nC);
+      const float dts = BATCH ? S.dt : dt;
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
         st[(R::V + d) * cap + j] = vv[d];
-        x[d] = x[d] + dt * vv[d];
+        x[d] = x[d] + dts * vv[d];
         st[(R::X + d) * cap + j] = x[d];
       }
 #pragma unroll
@@ -1249,19 +1283,27 @@ __global__ __launch_bounds__(128, 5) void k_g2p_stream(const MpmParams P, const 
 #pragma unroll
       for (int d = 0; d < 3; ++d) vv[d] = st[(R::V + d) * cap + j];
     }
+    if (BATCH) {
+      const int sc = scene_index_of_particle(P, matword);
+      if (sc != vscene) {
+        if (maxv_out && vmax > 0.0f) atomicMax((int *)&maxv_out[vscene], __float_as_int(vmax));
+        vmax = 0.0f;
+        vscene = sc;
+      }
+    }
     vmax = fmaxf(vmax, fmaxf(fabsf(vv[0]), fmaxf(fabsf(vv[1]), fabsf(vv[2]))));
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       bmin[d] = fminf(bmin[d], x[d]);
       bmax[d] = fmaxf(bmax[d], x[d]);
     }
-    bin_one<false>(P, nullptr, w, j, x[0], x[1], x[2], matword, bad);
+    bin_one<BATCH>(P, tab, w, j, x[0], x[1], x[2], matword, bad);
   }
   set_status(w, bad);
-  if (maxv_out) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
-    if (lane == 0 && vmax > 0.0f) atomicMax((int *)maxv_out, __float_as_int(vmax));
+  flush_vmax<BATCH>(maxv_out, vmax, vscene, lane);
+  if (BATCH) {  // no bounding box: the batched window is fixed by its slots
+    step_queue_done(w, kFusedQueue, kFusedDone, lane, nwarps);
+    return;
   }
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
@@ -1598,16 +1640,17 @@ struct DevInfo {
   int p2g_b_ctas = 0, p2g_ep_b_ctas = 0, g2p_b_ctas = 0;
   int p2g_q_ctas = 0, p2g_ep_q_ctas = 0, g2p_q_ctas = 0, g2p2g_q_ctas = 0;  // packed storage
   int fused_ctas[2][3] = {{0, 0, 0}, {0, 0, 0}};  // k_fused [has_Ep][mode]
-  int g2ps_ctas = 0, binbox_ctas = 0;
+  int fused_b_ctas[2] = {0, 0};                    // batched k_fused [has_Ep]
+  int g2ps_ctas = 0, g2ps_b_ctas = 0, binbox_ctas = 0;
 };
 
-// CTAs of one full wave of k_fused<HAS_EP, MODE> (its dynamic shared memory
-// opted in first)
-template <bool HAS_EP, int MODE>
+// CTAs of one full wave of k_fused<HAS_EP, MODE, BATCH> (its dynamic shared
+// memory opted in first)
+template <bool HAS_EP, int MODE, bool BATCH = false>
 static void fused_occupancy(int sms, int &ctas) {
   int k = 0;
-  cudaFuncSetAttribute(k_fused<HAS_EP, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFusedSmem);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, k_fused<HAS_EP, MODE>, kP2GThreads, kFusedSmem);
+  cudaFuncSetAttribute(k_fused<HAS_EP, MODE, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFusedSmem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, k_fused<HAS_EP, MODE, BATCH>, kP2GThreads, kFusedSmem);
   ctas = sms * (k > 0 ? k : 1);
 }
 
@@ -1653,10 +1696,14 @@ static const DevInfo *dev_info() {
       fused_occupancy<true, kFusedG2P2G>(sms, d.fused_ctas[1][1]);
       fused_occupancy<false, kFusedG2P2GSorted>(sms, d.fused_ctas[0][2]);
       fused_occupancy<true, kFusedG2P2GSorted>(sms, d.fused_ctas[1][2]);
-      int gs = 0, bb = 0;
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&gs, k_g2p_stream, 128, 0);
+      fused_occupancy<false, kFusedPlain, true>(sms, d.fused_b_ctas[0]);
+      fused_occupancy<true, kFusedPlain, true>(sms, d.fused_b_ctas[1]);
+      int gs = 0, gsb = 0, bb = 0;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&gs, k_g2p_stream<false>, 128, 0);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&gsb, k_g2p_stream<true>, 128, 0);
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bb, k_bin_box, 256, 0);
       d.g2ps_ctas = sms * (gs > 0 ? gs : 1);
+      d.g2ps_b_ctas = sms * (gsb > 0 ? gsb : 1);
       d.binbox_ctas = sms * (bb > 0 ? bb : 1);
     }
     d.sms = sms;
@@ -1870,31 +1917,38 @@ int mpm_substep(const MpmParams *p, void *ws, int64_t cap, int64_t n, const floa
 
 // The particle kernel of a fused substep on `st`: the G2P of the previous
 // substep, advection, the constitutive update and the P2G of this one (MODE:
-// the plain loop in place, or the G2P2G mode in place or into `out` sorted).
+// the plain loop in place, or the G2P2G mode in place or into `out` sorted;
+// BATCH: the plain loop over the scenes of a batch, `tab` their parameters).
 extern "C++" {
-template <int MODE>
-static int fused_particles(const DevInfo *di, cudaStream_t s, const MpmParams &p, const Ws &w, float *st, float *out,
-                           int64_t cap, int64_t n, float dt, int64_t first_new, float *maxv) {
+template <int MODE, bool BATCH = false>
+static int fused_particles(const DevInfo *di, cudaStream_t s, const MpmParams &p, const MpmParams *tab, const Ws &w,
+                           float *st, float *out, int64_t cap, int64_t n, float dt, int64_t first_new, float *maxv) {
   CUtensorMap mx, mf;
   const int nf = p.has_Ep ? kFusedRowsF : (MODE == kFusedG2P2GSorted ? kFusedRowsF - 1 : kFusedRowsF - 2);
   if (!rows_tensor_map(&mx, st, cap, MPM_NROWS, 3) || !rows_tensor_map(&mf, st, cap, MPM_NROWS, nf))
     return MPM_E_CUDA;
+  const int ctas = BATCH ? di->fused_b_ctas[p.has_Ep ? 1 : 0] : di->fused_ctas[p.has_Ep ? 1 : 0][MODE];
   if (p.has_Ep)
-    k_fused<true, MODE><<<di->fused_ctas[1][MODE], kP2GThreads, kFusedSmem, s>>>(p, w, mx, mf, st, out, cap, n, dt,
-                                                                                  first_new, maxv);
+    k_fused<true, MODE, BATCH><<<ctas, kP2GThreads, kFusedSmem, s>>>(p, tab, w, mx, mf, st, out, cap, n, dt,
+                                                                    first_new, maxv);
   else
-    k_fused<false, MODE><<<di->fused_ctas[0][MODE], kP2GThreads, kFusedSmem, s>>>(p, w, mx, mf, st, out, cap, n, dt,
-                                                                                   first_new, maxv);
+    k_fused<false, MODE, BATCH><<<ctas, kP2GThreads, kFusedSmem, s>>>(p, tab, w, mx, mf, st, out, cap, n, dt,
+                                                                     first_new, maxv);
   return MPM_OK;
 }
 }  // extern "C++"
 
 // The grid half of a fused substep: the blocks the particles marked become
-// the grid-active list, then the grid update over them.
-static void fused_grid(cudaStream_t s, const DevInfo *di, const MpmParams &p, const Ws &w, float dt) {
+// the grid-active list, then the grid update over them (`tab`: the scene
+// table of a batch, else null).
+static void fused_grid(cudaStream_t s, const DevInfo *di, const MpmParams &p, const MpmParams *tab, const Ws &w,
+                       float dt) {
   k_flags_count<<<w.nflagtiles, 256, 0, s>>>(p, w);
   k_flags_write<<<w.nflagtiles, 256, 0, s>>>(p, w);
-  k_grid<false><<<di->sms * 8, 256, 0, s>>>(p, nullptr, w, dt);
+  if (tab)
+    k_grid<true><<<di->sms * 8, 256, 0, s>>>(p, tab, w, 0.0f);
+  else
+    k_grid<false><<<di->sms * 8, 256, 0, s>>>(p, nullptr, w, dt);
 }
 
 static bool batch_ok(const MpmParams *p) {
@@ -1975,18 +2029,21 @@ int mpm_substep_noalloc(const MpmParams *p, int64_t cap, int64_t n, const float 
   return last_error();
 }
 
-// The frame driver of mpm_frame (G2P2G false) and mpm_g2p2g_frame.
+// The frame driver of mpm_frame (G2P2G false), mpm_g2p2g_frame and, with a
+// scene table `tab`, mpm_batch_frame (the plain loop over a batch; `maxv`
+// then holds n_scenes floats per substep).
 // events[5k + j]: substep k's start, after the binning of the state (a sort
 // substep of the G2P2G mode) or the closing G2P of the previous plain run,
 // after the finalize, after the particle kernel, after the grid update;
 // events[5 count], [5 count + 1] bracket the frame's closing pass.
 extern "C++" {
-template <bool G2P2G>
-static int run_frame(const MpmParams *p, void *ws, int64_t cap, int64_t n, float *a, float *b, float dt,
-                     int32_t count, int32_t resort, int64_t first_new, float *maxv, int32_t *in_b,
+template <bool G2P2G, bool BATCH>
+static int run_frame(const MpmParams *p, const MpmParams *tab, void *ws, int64_t cap, int64_t n, float *a, float *b,
+                     float dt, int32_t count, int32_t resort, int64_t first_new, float *maxv, int32_t *in_b,
                      void *const *events, void *stream) {
-  if (!params_ok(p) || p->quant || p->n_scenes > 0 || !ws || !a || !b || !maxv || !in_b || n < 0 || n > cap ||
-      count < 1 || resort < 1 || first_new < 0 || !p2g_rows_ok(a, cap) || !p2g_rows_ok(b, cap))
+  const bool params = BATCH ? (batch_ok(p) && tab != nullptr) : (params_ok(p) && p->n_scenes == 0);
+  if (!params || p->quant || !ws || !a || !b || !maxv || !in_b || n < 0 || n > cap || count < 1 || resort < 1 ||
+      first_new < 0 || !p2g_rows_ok(a, cap) || !p2g_rows_ok(b, cap))
     return MPM_E_INVALID;
   const DevInfo *di = dev_info();
   if (!di) return MPM_E_CUDA;
@@ -1995,6 +2052,13 @@ static int run_frame(const MpmParams *p, void *ws, int64_t cap, int64_t n, float
   cudaStream_t s = (cudaStream_t)stream;
   auto mark = [&](int64_t e) {
     if (events) cudaEventRecord((cudaEvent_t)events[e], s);
+  };
+  const int64_t mv_stride = BATCH ? p->n_scenes : 1;  // maxv floats per substep
+  auto close_g2p = [&](float *st, float *mv) {
+    if (BATCH)
+      k_g2p_stream<true><<<di->g2ps_b_ctas, 128, 0, s>>>(*p, tab, w, st, cap, n, dt, mv);
+    else
+      k_g2p_stream<false><<<di->g2ps_ctas, 128, 0, s>>>(*p, nullptr, w, st, cap, n, dt, mv);
   };
   float *cur = a, *oth = b;
   int rc = MPM_OK;
@@ -2008,7 +2072,7 @@ static int run_frame(const MpmParams *p, void *ws, int64_t cap, int64_t n, float
         if (G2P2G)
           k_bin_box<<<di->binbox_ctas, 256, 0, s>>>(*p, w, cur, cap, n, 0);
         else
-          k_g2p_stream<<<di->g2ps_ctas, 128, 0, s>>>(*p, w, cur, cap, n, dt, maxv + k - 1);
+          close_g2p(cur, maxv + (k - 1) * mv_stride);
       }
       mark(5 * k + 1);
       rc = mpm_bin_finalize(p, ws, cap, n, stream);
@@ -2016,17 +2080,24 @@ static int run_frame(const MpmParams *p, void *ws, int64_t cap, int64_t n, float
       mark(5 * k + 2);
       if (G2P2G) {
         if (n > 0) {
-          rc = fused_particles<kFusedG2P2GSorted>(di, s, *p, w, cur, oth, cap, n, dt, k == 0 ? first_new : n,
-                                                  maxv + k);
+          rc = fused_particles<kFusedG2P2GSorted>(di, s, *p, nullptr, w, cur, oth, cap, n, dt,
+                                                  k == 0 ? first_new : n, maxv + k);
           if (rc) return rc;
         }
         mark(5 * k + 3);
-        fused_grid(s, di, *p, w, dt);
+        fused_grid(s, di, *p, nullptr, w, dt);
       } else {
-        rc = launch_p2g_single(di, s, *p, w, cur, oth, cap, n, dt);
+        if (BATCH)
+          rc = p->has_Ep ? launch_p2g<true, true, false>(di->p2g_ep_b_ctas, s, *p, tab, w, cur, oth, cap, n, 0.0f)
+                         : launch_p2g<false, true, false>(di->p2g_b_ctas, s, *p, tab, w, cur, oth, cap, n, 0.0f);
+        else
+          rc = launch_p2g_single(di, s, *p, w, cur, oth, cap, n, dt);
         if (rc) return rc;
         mark(5 * k + 3);
-        k_grid<false><<<di->sms * 8, 256, 0, s>>>(*p, nullptr, w, dt);
+        if (BATCH)
+          k_grid<true><<<di->sms * 8, 256, 0, s>>>(*p, tab, w, 0.0f);
+        else
+          k_grid<false><<<di->sms * 8, 256, 0, s>>>(*p, nullptr, w, dt);
       }
       float *t = cur;
       cur = oth;
@@ -2035,13 +2106,16 @@ static int run_frame(const MpmParams *p, void *ws, int64_t cap, int64_t n, float
       mark(5 * k + 1);
       mark(5 * k + 2);
       if (n > 0) {
-        rc = G2P2G ? fused_particles<kFusedG2P2G>(di, s, *p, w, cur, nullptr, cap, n, dt, k == 0 ? first_new : n,
-                                                  maxv + k)
-                   : fused_particles<kFusedPlain>(di, s, *p, w, cur, nullptr, cap, n, dt, 0, maxv + k - 1);
+        if (G2P2G)
+          rc = fused_particles<kFusedG2P2G>(di, s, *p, nullptr, w, cur, nullptr, cap, n, dt, k == 0 ? first_new : n,
+                                            maxv + k);
+        else
+          rc = fused_particles<kFusedPlain, BATCH>(di, s, *p, tab, w, cur, nullptr, cap, n, dt, 0,
+                                                   maxv + (k - 1) * mv_stride);
         if (rc) return rc;
       }
       mark(5 * k + 3);
-      if (n > 0) fused_grid(s, di, *p, w, dt);
+      if (n > 0) fused_grid(s, di, *p, BATCH ? tab : nullptr, w, dt);
     }
     mark(5 * k + 4);
   }
@@ -2050,7 +2124,7 @@ static int run_frame(const MpmParams *p, void *ws, int64_t cap, int64_t n, float
     if (G2P2G)
       k_bin_box<<<di->binbox_ctas, 256, 0, s>>>(*p, w, cur, cap, n, 1);
     else
-      k_g2p_stream<<<di->g2ps_ctas, 128, 0, s>>>(*p, w, cur, cap, n, dt, maxv + count - 1);
+      close_g2p(cur, maxv + (count - 1) * mv_stride);
   }
   mark(5 * (int64_t)count + 1);
   *in_b = cur == b;
@@ -2058,15 +2132,23 @@ static int run_frame(const MpmParams *p, void *ws, int64_t cap, int64_t n, float
 }
 }  // extern "C++"
 
+
 int mpm_frame(const MpmParams *p, void *ws, int64_t cap, int64_t n, float *a, float *b, float dt, int32_t count,
               int32_t resort, float *maxv, int32_t *in_b, void *const *events, void *stream) {
-  return run_frame<false>(p, ws, cap, n, a, b, dt, count, resort, 0, maxv, in_b, events, stream);
+  return run_frame<false, false>(p, nullptr, ws, cap, n, a, b, dt, count, resort, 0, maxv, in_b, events, stream);
+}
+
+int mpm_batch_frame(const MpmParams *p, const MpmParams *scenes, void *ws, int64_t cap, int64_t n, float *a,
+                    float *b, int32_t count, int32_t resort, float *maxv, int32_t *in_b, void *const *events,
+                    void *stream) {
+  return run_frame<false, true>(p, scenes, ws, cap, n, a, b, 0.0f, count, resort, 0, maxv, in_b, events, stream);
 }
 
 int mpm_g2p2g_frame(const MpmParams *p, void *ws, int64_t cap, int64_t n, float *a, float *b, float dt,
                     int32_t count, int32_t resort, int64_t first_new, float *maxv, int32_t *in_b,
                     void *const *events, void *stream) {
-  return run_frame<true>(p, ws, cap, n, a, b, dt, count, resort, first_new, maxv, in_b, events, stream);
+  return run_frame<true, false>(p, nullptr, ws, cap, n, a, b, dt, count, resort, first_new, maxv, in_b, events,
+                                stream);
 }
 
 int mpm_max_grid_velocity(const MpmParams *p, void *ws, int64_t cap, float *out, void *stream) {

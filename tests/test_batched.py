@@ -124,3 +124,30 @@ def test_batched_64_scenes_match_oracle():
                 worst[k] = errs[k]
     print(f"\nworst over {len(bs)} scenes: x {worst['x'][0]:.2e} (f32 {worst['x'][1]:.1e}), "
           f"v {worst['v'][0]:.2e} (f32 {worst['v'][1]:.1e})")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("resort", [1, 3, 24])
+def test_batched_frames_match_per_substep_launches(resort):
+    """mpm_batch_frame (fused frames, re-sorted about every `resort`
+    substeps) against the batch's per-substep launches: the same arithmetic
+    in another order, so positions agree to float32 rounding and every
+    scene's max |v| per substep matches."""
+    from taichi_elements_gb300._lib import ROW_X
+    from taichi_elements_gb300.batched import BatchedMPM
+    bs = small_scenes()
+    a = BatchedMPM(bs, use_cuda_graph=False)
+    b = BatchedMPM(bs, use_cuda_graph=False)
+    a.fuse_frames = True
+    a.resort_every = resort
+    b.fuse_frames = False
+    nsub = 10
+    a.substeps(nsub)
+    b.substeps(nsub)
+    a.check_status()
+    b.check_status()
+    xa, xb = a._gather(ROW_X, 3).cpu().numpy(), b._gather(ROW_X, 3).cpu().numpy()
+    assert np.abs(xa - xb).max() < 1e-5
+    ma, mb = a.max_velocity(nsub), b.max_velocity(nsub)
+    assert ma.shape == (nsub, len(bs))
+    assert np.allclose(ma, mb, rtol=1e-4, atol=1e-6)

@@ -7,7 +7,7 @@ Default workload: the large sparse scene, 16M particles in 64 ellipsoids on
 a 256^3 grid (elastic/snow, ground collider), seeded synthetic inputs.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--workload ellipsoids_256|four_materials_128|water_cube_64]
+                  [--workload ellipsoids_256|four_materials_128|water_cube_64|batched_64|elastic_on_water]
 
 Prints one JSON line.  `value` times K substeps with state resident in HBM,
 run as frames through mpm_frame (the kernels MPMSolver.step runs: fused
@@ -995,7 +995,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=None)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="ellipsoids_256",
-                    choices=["ellipsoids_256", "four_materials_128", "water_cube_64", "elastic_on_water"])
+                    choices=["ellipsoids_256", "four_materials_128", "water_cube_64", "elastic_on_water",
+                             "batched_64"])
     ap.add_argument("--chunk", type=int, default=None)
     ap.add_argument("--resort", type=int, default=None, help="fused frames re-sorted every this many substeps")
     ap.add_argument("--frame", type=int, default=50, help="substeps per mpm_frame call in the timed region")
@@ -1017,6 +1018,9 @@ def main():
     args = ap.parse_args()
     if args.workload == "elastic_on_water":  # the differentiable workload alone
         print(json.dumps(run_adjoint_measure(n_substeps=args.steps or 2000)))
+        return
+    if args.workload == "batched_64":  # the 64-scene batched workload alone
+        print(json.dumps(run_batched_measure()))
         return
     if args.impl == "reference":
         args.steps = 3 if args.steps is None else args.steps

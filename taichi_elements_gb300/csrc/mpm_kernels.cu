@@ -1038,7 +1038,10 @@ __device__ __forceinline__ void flush_vmax(float *maxv_out, float vmax, int vsce
 // P2G of substep s), and the G2P2G mode (engine/mpm_solver.py:363-485) in
 // place or writing every state row to the particle's sorted slot inv[i] of
 // another buffer (the substep that re-sorts).
-constexpr int kFusedPlain = 0, kFusedG2P2G = 1, kFusedG2P2GSorted = 2;
+// In place the G2P2G mode stores v only at a frame's last substep
+// (kFusedG2P2GLast): the next substep gathers v afresh, except for stationary
+// particles, whose stored v never changes.
+constexpr int kFusedPlain = 0, kFusedG2P2G = 1, kFusedG2P2GSorted = 2, kFusedG2P2GLast = 3;
 
 template <bool HAS_EP, int MODE, bool BATCH = false>
 __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_fused(const MpmParams P, const MpmParams *tab,
@@ -1143,11 +1146,11 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_fused(const M
         if (mat != 4) {
 #pragma unroll
           for (int d = 0; d < 3; ++d) x[d] = x[d] + dt * v[d];
-          if (!SORTED) {  // in place: x and v (unchanged for a fresh particle) now
+          if (!SORTED) {  // in place: x now, v at the frame's last substep
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
               st[(R::X + d) * cap + i] = x[d];
-              st[(R::V + d) * cap + i] = v[d];
+              if (MODE == kFusedG2P2GLast) st[(R::V + d) * cap + i] = v[d];
             }
           }
         }
@@ -1639,7 +1642,7 @@ struct DevInfo {
   int p2g_ctas = 0, p2g_ep_ctas = 0, g2p_ctas = 0, g2p2g_ctas = 0;
   int p2g_b_ctas = 0, p2g_ep_b_ctas = 0, g2p_b_ctas = 0;
   int p2g_q_ctas = 0, p2g_ep_q_ctas = 0, g2p_q_ctas = 0, g2p2g_q_ctas = 0;  // packed storage
-  int fused_ctas[2][3] = {{0, 0, 0}, {0, 0, 0}};  // k_fused [has_Ep][mode]
+  int fused_ctas[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};  // k_fused [has_Ep][mode]
   int fused_b_ctas[2] = {0, 0};                    // batched k_fused [has_Ep]
   int g2ps_ctas = 0, g2ps_b_ctas = 0, binbox_ctas = 0;
 };
@@ -1696,6 +1699,8 @@ static const DevInfo *dev_info() {
       fused_occupancy<true, kFusedG2P2G>(sms, d.fused_ctas[1][1]);
       fused_occupancy<false, kFusedG2P2GSorted>(sms, d.fused_ctas[0][2]);
       fused_occupancy<true, kFusedG2P2GSorted>(sms, d.fused_ctas[1][2]);
+      fused_occupancy<false, kFusedG2P2GLast>(sms, d.fused_ctas[0][3]);
+      fused_occupancy<true, kFusedG2P2GLast>(sms, d.fused_ctas[1][3]);
       fused_occupancy<false, kFusedPlain, true>(sms, d.fused_b_ctas[0]);
       fused_occupancy<true, kFusedPlain, true>(sms, d.fused_b_ctas[1]);
       int gs = 0, gsb = 0, bb = 0;
@@ -2107,8 +2112,10 @@ static int run_frame(const MpmParams *p, const MpmParams *tab, void *ws, int64_t
       mark(5 * k + 2);
       if (n > 0) {
         if (G2P2G)
-          rc = fused_particles<kFusedG2P2G>(di, s, *p, nullptr, w, cur, nullptr, cap, n, dt, k == 0 ? first_new : n,
-                                            maxv + k);
+          rc = k + 1 < count ? fused_particles<kFusedG2P2G>(di, s, *p, nullptr, w, cur, nullptr, cap, n, dt,
+                                                            k == 0 ? first_new : n, maxv + k)
+                             : fused_particles<kFusedG2P2GLast>(di, s, *p, nullptr, w, cur, nullptr, cap, n, dt,
+                                                                k == 0 ? first_new : n, maxv + k);
         else
           rc = fused_particles<kFusedPlain, BATCH>(di, s, *p, tab, w, cur, nullptr, cap, n, dt, 0,
                                                    maxv + (k - 1) * mv_stride);

@@ -1025,13 +1025,13 @@ __device__ __forceinline__ int scene_index_of_particle(const MpmParams &P, int m
 template <bool BATCH>
 __device__ __forceinline__ void flush_vmax(float *maxv_out, float vmax, int vscene, int lane) {
   if (!maxv_out) return;
-  if (BATCH) {
+  if constexpr (BATCH) {
     if (vmax > 0.0f) atomicMax((int *)&maxv_out[vscene], __float_as_int(vmax));
-    return;
-  }
+  } else {
 #pragma unroll
-  for (int d = 16; d > 0; d >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, d));
-  if (lane == 0 && vmax > 0.0f) atomicMax((int *)maxv_out, __float_as_int(vmax));
+    for (int d = 16; d > 0; d >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, d));
+    if (lane == 0 && vmax > 0.0f) atomicMax((int *)maxv_out, __float_as_int(vmax));
+  }
 }
 
 // Modes of the fused kernel: the plain loop in place (G2P of substep s-1,
@@ -1304,20 +1304,18 @@ __global__ __launch_bounds__(128, 5) void k_g2p_stream(const MpmParams P, const 
   }
   set_status(w, bad);
   flush_vmax<BATCH>(maxv_out, vmax, vscene, lane);
-  if (BATCH) {  // no bounding box: the batched window is fixed by its slots
-    step_queue_done(w, kFusedQueue, kFusedDone, lane, nwarps);
-    return;
-  }
+  if constexpr (!BATCH) {  // the batched window is fixed by its slots: no bounding box
 #pragma unroll
-  for (int d = 0; d < 3; ++d) {
+    for (int d = 0; d < 3; ++d) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      bmin[d] = fminf(bmin[d], __shfl_xor_sync(0xffffffffu, bmin[d], o));
-      bmax[d] = fmaxf(bmax[d], __shfl_xor_sync(0xffffffffu, bmax[d], o));
-    }
-    if (lane == 0 && bmin[d] <= bmax[d]) {
-      atomicMin(&w.counters[kBoxMin + d], float_key_i32(bmin[d]));
-      atomicMax(&w.counters[kBoxMax + d], float_key_i32(bmax[d]));
+      for (int o = 16; o > 0; o >>= 1) {
+        bmin[d] = fminf(bmin[d], __shfl_xor_sync(0xffffffffu, bmin[d], o));
+        bmax[d] = fmaxf(bmax[d], __shfl_xor_sync(0xffffffffu, bmax[d], o));
+      }
+      if (lane == 0 && bmin[d] <= bmax[d]) {
+        atomicMin(&w.counters[kBoxMin + d], float_key_i32(bmin[d]));
+        atomicMax(&w.counters[kBoxMax + d], float_key_i32(bmax[d]));
+      }
     }
   }
   step_queue_done(w, kFusedQueue, kFusedDone, lane, nwarps);

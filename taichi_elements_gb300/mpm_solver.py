@@ -35,6 +35,7 @@ from __future__ import annotations
 import ctypes
 import math
 import numbers
+import sys
 import time
 
 import numpy as np
@@ -62,6 +63,42 @@ class ParticleCount(int):
         if key is None or key == ():
             return int(self)
         raise TypeError("n_particles is a scalar: index it with [None]")
+
+
+# Page-locked host buffers for device-to-host copies, shared by all
+# solvers of the process: pairs of a pinned tensor and the numpy array that
+# views it.  The numpy array is what callers receive; it (or any numpy view
+# of it) is referenced while a caller holds it, and a pair is handed out
+# again only when nothing but the pool references its array, so every
+# returned array stays the caller's own, as the reference's fresh copies are.
+# Unused pairs are dropped, oldest first, above _PINNED_POOL_BYTES.
+_pinned_pool: list = []
+_PINNED_POOL_BYTES = 8 << 30
+
+
+def _pinned_buffer(shape, dtype):
+    """A free (pinned tensor, numpy view) pair of this shape and dtype."""
+    shape = tuple(shape)
+    for pair in _pinned_pool:
+        h, hn = pair
+        # held by the pool alone: the pair, the local name, getrefcount's argument
+        if h.dtype == dtype and tuple(h.shape) == shape and sys.getrefcount(hn) <= 3:
+            return pair
+    h = hn = pair = None  # the loop's names must not keep a pool array referenced
+    h = torch.empty(shape, dtype=dtype, pin_memory=True)
+    pair = (h, h.numpy())
+    _pinned_pool.append(pair)
+    total = sum(q[0].numel() * q[0].element_size() for q in _pinned_pool)
+    i = 0
+    while total > _PINNED_POOL_BYTES and i < len(_pinned_pool):
+        q = _pinned_pool[i]
+        if q is not pair and sys.getrefcount(q[1]) <= 2:  # the pair and the argument
+            total -= q[0].numel() * q[0].element_size()
+            del _pinned_pool[i]
+        else:
+            i += 1
+        q = None
+    return pair
 
 
 def frame_resort_interval(count: int, target: int) -> int:
@@ -980,16 +1017,17 @@ class MPMSolver:
         return dict(zip(dev.keys(), self._to_host(*dev.values())))
 
     def _to_host(self, *tensors):
-        """numpy copies of device tensors through page-locked buffers (the
-        caching host allocator reuses them across frames), one
-        synchronisation for all."""
+        """numpy copies of device tensors through page-locked buffers, one
+        synchronisation for all.  The buffers come from a process-wide pool
+        (_pinned_buffer): pinning fresh host memory costs about 13 GB/s, a
+        copy into pinned memory ~180 GB/s on GB300."""
         host = []
         for t in tensors:
-            h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+            h, hn = _pinned_buffer(t.shape, t.dtype)
             h.copy_(t, non_blocking=True)
-            host.append(h)
+            host.append(hn)
         torch.cuda.current_stream(self.device).synchronize()
-        return [h.numpy() for h in host]
+        return host
 
     def full_state(self):
         """All particle fields in original order as float32 device tensors:

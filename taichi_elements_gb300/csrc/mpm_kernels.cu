@@ -1146,13 +1146,6 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_fused(const M
         if (mat != 4) {
 #pragma unroll
           for (int d = 0; d < 3; ++d) x[d] = x[d] + dt * v[d];
-          if (!SORTED) {  // in place: x now, v at the frame's last substep
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-              st[(R::X + d) * cap + i] = x[d];
-              if (MODE == kFusedG2P2GLast) st[(R::V + d) * cap + i] = v[d];
-            }
-          }
         }
       }
       const float vm = fmaxf(fabsf(v[0]), fmaxf(fabsf(v[1]), fabsf(v[2])));
@@ -1177,6 +1170,13 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_fused(const M
 #pragma unroll
       for (int a = 0; a < 9; ++a) dst[(R::F + a) * cap + j] = F[a / 3][a % 3];
       dst[R::Jp * cap + j] = Jp;
+      if (G2P2G && !SORTED && mat != 4) {  // in place: x, and v at the frame's last substep
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          dst[(R::X + d) * cap + j] = x[d];
+          if (MODE == kFusedG2P2GLast) dst[(R::V + d) * cap + j] = v[d];
+        }
+      }
       if (SORTED) {
 #pragma unroll
         for (int d = 0; d < 3; ++d) {

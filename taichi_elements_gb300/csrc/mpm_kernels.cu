@@ -1123,10 +1123,7 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_fused(const M
         if (mat != 4) {
           gather_vc(P, S.inv_dx, w.grid_vel, b0, v, C);
 #pragma unroll
-          for (int d = 0; d < 3; ++d) {
-            x[d] = x[d] + dts * v[d];
-            st[(R::X + d) * cap + i] = x[d];
-          }
+          for (int d = 0; d < 3; ++d) x[d] = x[d] + dts * v[d];
         } else {  // stationary: v, C and x stay
 #pragma unroll
           for (int d = 0; d < 3; ++d) v[d] = st[(R::V + d) * cap + i];
@@ -1170,6 +1167,10 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_fused(const M
 #pragma unroll
       for (int a = 0; a < 9; ++a) dst[(R::F + a) * cap + j] = F[a / 3][a % 3];
       dst[R::Jp * cap + j] = Jp;
+      if (!G2P2G && mat != 4) {  // the advected x
+#pragma unroll
+        for (int d = 0; d < 3; ++d) dst[(R::X + d) * cap + j] = x[d];
+      }
       if (G2P2G && !SORTED && mat != 4) {  // in place: x, and v at the frame's last substep
 #pragma unroll
         for (int d = 0; d < 3; ++d) {

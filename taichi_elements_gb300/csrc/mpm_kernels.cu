@@ -501,7 +501,10 @@ __device__ __forceinline__ void p2g_tile_flush(const MpmParams &P, const Ws &w, 
 // tile is anchored at the step's base cells (see k_p2g); a particle outside a
 // fresh anchor scatters with global atomics.  MARK: flag the blocks that
 // receive momentum (see p2g_tile_flush).
-template <bool MARK>
+// ROLL keeps the stencil's x loop rolled: fewer registers (the batched P2G
+// then fits 4 CTAs per SM, 16 warps, and runs 10% faster on the batch's small
+// scenes) for a longer instruction stream.
+template <bool MARK, bool ROLL = false>
 __device__ __forceinline__ void p2g_scatter_step(const MpmParams &P, const Ws &w, float4 *tile, int (&o)[3],
                                                  bool &anchored, bool act, const Base &bs, const float (&wt)[3][3],
                                                  float mass, const float (&q)[3], const float (&adx)[3][3],
@@ -556,14 +559,16 @@ __device__ __forceinline__ void p2g_scatter_step(const MpmParams &P, const Ws &w
   const int base_node = inwin ? cell : 0;
   for (int round = 0;; ++round) {
     const bool mine = inwin && round_of_lane == round;
-#pragma unroll
+#pragma unroll(ROLL ? 1 : 3)
     for (int a = 0; a < 3; ++a)
 #pragma unroll
       for (int bb = 0; bb < 3; ++bb) {
-        const float wab = wt[a][0] * wt[bb][1];
-        const float2 p0 = make_float2(mass, fmaf(adx[0][1], (float)bb, fmaf(adx[0][0], (float)a, q[0])));
-        const float2 p1 = make_float2(fmaf(adx[1][1], (float)bb, fmaf(adx[1][0], (float)a, q[1])),
-                                      fmaf(adx[2][1], (float)bb, fmaf(adx[2][0], (float)a, q[2])));
+        const float wxa = a == 0 ? wt[0][0] : (a == 1 ? wt[1][0] : wt[2][0]);  // no indexing by a rolled a
+        const float fa = (float)a;
+        const float wab = wxa * wt[bb][1];
+        const float2 p0 = make_float2(mass, fmaf(adx[0][1], (float)bb, fmaf(adx[0][0], fa, q[0])));
+        const float2 p1 = make_float2(fmaf(adx[1][1], (float)bb, fmaf(adx[1][0], fa, q[1])),
+                                      fmaf(adx[2][1], (float)bb, fmaf(adx[2][0], fa, q[2])));
         const float2 dz0 = make_float2(0.0f, adx[0][2]), dz1 = make_float2(adx[1][2], adx[2][2]);
         float2 t0 = p0, t1 = p1;
 #pragma unroll
@@ -740,7 +745,7 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_p2g(const Mpm
 #pragma unroll
         for (int c = 0; c < 3; ++c) adx[r][c] = out.affine[r][c] * S.dx;
     }
-    p2g_scatter_step<false>(P, w, sm.tile, o, anchored, act, bs, wt, mass, q, adx, lane);
+    p2g_scatter_step<false, BATCH>(P, w, sm.tile, o, anchored, act, bs, wt, mass, q, adx, lane);
     g0 = g1;
   }
   if (anchored) p2g_tile_flush<false>(P, w, sm.tile, o, lane);

@@ -46,7 +46,7 @@
 extern "C" {
 #endif
 
-#define MPM_ABI_VERSION 5
+#define MPM_ABI_VERSION 6
 #define MPM_NROWS 28
 #define MPM_QROWS 21
 #define MPM_MAX_COLLIDERS 16 /* post-process records, box included */
@@ -99,6 +99,12 @@ typedef struct MpmParams {
                        * carries no stress */
   int32_t quant;      /* quant=True (mpm_solver.py:106-127, :216-262): pstate
                        * holds the packed 21-row layout (MPM_QROWS) */
+  int32_t occupancy;  /* register budget of the fused and streaming P2G
+                       * kernels: 0 = stencil loops fully unrolled, 3 CTAs
+                       * (12 warps) per SM; 1 = their x loops rolled, 4 CTAs
+                       * (16 warps) per SM.  Results are the same; which is
+                       * faster depends on the scene (measured per scene by
+                       * the Python autotuner) */
   float dx, inv_dx, p_vol, p_mass;
   float mu0, la0, nu, alpha; /* Lame parameters, Poisson ratio, sand alpha */
   float water_density;

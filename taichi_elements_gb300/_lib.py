@@ -12,7 +12,7 @@ from pathlib import Path
 
 from . import build as _build
 
-ABI_VERSION = 5
+ABI_VERSION = 6
 NROWS = 28
 QROWS = 21  # packed rows of quant=True (MPM_QROWS)
 MAX_COLLIDERS = 16
@@ -57,6 +57,7 @@ class MpmParams(ctypes.Structure):
         ("chunk", ctypes.c_int32),
         ("plasticity", ctypes.c_int32),
         ("quant", ctypes.c_int32),
+        ("occupancy", ctypes.c_int32),
         ("dx", ctypes.c_float),
         ("inv_dx", ctypes.c_float),
         ("p_vol", ctypes.c_float),

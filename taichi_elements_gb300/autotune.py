@@ -15,8 +15,9 @@ arithmetic:
   sorts save the sort's data movement.
 
 ``tune_chunk`` times the chunk candidates; ``tune_schedule`` times fused
-frames for each re-sort candidate against the per-substep schedule at its
-best chunk and applies the fastest.  Both run on a scratch copy of the
+frames for each re-sort candidate, with the fused kernels' stencil loops
+unrolled (12 warps per SM) and rolled (16 warps per SM, MpmParams.occupancy),
+against the per-substep schedule at its best chunk and applies the fastest.  Both run on a scratch copy of the
 solver's particles (the simulation itself is not advanced).  Results are
 cached in memory per (device, particle-count bucket, grid resolution,
 per-particle E, material mix), and in the JSON file named by the
@@ -142,10 +143,11 @@ def tune_chunk(solver, candidates=CANDIDATES, substeps=8) -> int:
     return int(best)
 
 
-def time_frames(solver, candidates=RESORT_CANDIDATES, substeps=48, dt=None):
+def time_frames(solver, candidates=RESORT_CANDIDATES, substeps=48, dt=None, occupancy=0):
     """Milliseconds per substep of a fused frame of `substeps` substeps for
     each target re-sort interval (spread over the frame as step() spreads
-    it), measured on a copy."""
+    it), with the kernels' register budget `occupancy` (MpmParams.occupancy),
+    measured on a copy."""
     from .mpm_solver import frame_resort_interval
     solver._prepare(dt or solver.default_dt)
     dt = float(dt or solver.default_dt)
@@ -156,6 +158,7 @@ def time_frames(solver, candidates=RESORT_CANDIDATES, substeps=48, dt=None):
     maxv = torch.zeros(substeps, dtype=torch.float32, device=solver.device)
     stream = torch.cuda.current_stream(solver.device)
     p = _lib.MpmParams.from_buffer_copy(solver.params)
+    p.occupancy = int(occupancy)
     pp = ctypes.byref(p)
     out = {}
     for r in candidates:
@@ -206,17 +209,22 @@ def tune_schedule(solver, resort_candidates=RESORT_CANDIDATES, chunk_candidates=
         chunks = time_chunks(solver, chunk_candidates, substeps=8)
         chunk = min(chunks, key=chunks.get)
         frames = {} if solver.quant else time_frames(solver, resort_candidates, substeps)
+        rolled = {} if solver.quant else time_frames(solver, resort_candidates, substeps, occupancy=1)
         best = {"chunk": int(chunk), "substep_ms": {str(c): t for c, t in chunks.items()},
-                "frame_ms": {str(r): t for r, t in frames.items()}}
-        if frames and min(frames.values()) < chunks[chunk]:
-            best.update(mode="frame", resort=int(min(frames, key=frames.get)))
+                "frame_ms": {str(r): t for r, t in frames.items()},
+                "frame_ms_rolled": {str(r): t for r, t in rolled.items()}}
+        options = [(t, r, 0) for r, t in frames.items()] + [(t, r, 1) for r, t in rolled.items()]
+        if options and min(options)[0] < chunks[chunk]:
+            _, r, occ = min(options)
+            best.update(mode="frame", resort=int(r), occupancy=int(occ))
         else:
-            best.update(mode="substep", resort=int(solver.resort_every))
+            best.update(mode="substep", resort=int(solver.resort_every), occupancy=0)
         with _lock:
             _cache[key] = best
             _save_file()
     solver.fuse_frames = best["mode"] == "frame"
     solver.resort_every = int(best["resort"])
+    solver.occupancy = int(best.get("occupancy", 0))
     if solver.chunk != best["chunk"]:
         solver.chunk = int(best["chunk"])
         solver._invalidate_params()

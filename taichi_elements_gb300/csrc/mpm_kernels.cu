@@ -639,8 +639,11 @@ __device__ __forceinline__ void p2g_issue(P2GWarpSmem &sm, const CUtensorMap &ro
   }
 }
 
-template <bool HAS_EP, bool BATCH, bool Q>
-__global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_p2g(const MpmParams P, const MpmParams *tab, const Ws w,
+// ROLL: the scatter's x loop rolled, 4 CTAs per SM (MpmParams.occupancy; the
+// batched form always)
+template <bool HAS_EP, bool BATCH, bool Q, bool ROLL = BATCH>
+__global__ __launch_bounds__(kP2GThreads, ROLL ? 4 : MPM_P2G_MIN_CTAS) void k_p2g(const MpmParams P,
+                                                                                 const MpmParams *tab, const Ws w,
                                                         const __grid_constant__ CUtensorMap rows_map,
                                                         const float *__restrict__ cur, float *__restrict__ nxt,
                                                         int64_t cap, int64_t n, float dt) {
@@ -745,7 +748,7 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_p2g(const Mpm
 #pragma unroll
         for (int c = 0; c < 3; ++c) adx[r][c] = out.affine[r][c] * S.dx;
     }
-    p2g_scatter_step<false, BATCH>(P, w, sm.tile, o, anchored, act, bs, wt, mass, q, adx, lane);
+    p2g_scatter_step<false, ROLL>(P, w, sm.tile, o, anchored, act, bs, wt, mass, q, adx, lane);
     g0 = g1;
   }
   if (anchored) p2g_tile_flush<false>(P, w, sm.tile, o, lane);
@@ -956,6 +959,8 @@ __device__ __forceinline__ void stencil_addresses(const MpmParams &P, const int 
 }
 
 // G2P gather (:711-721) straight from the grid velocities: v and C.
+// ROLL: the x loop rolled (fewer registers, fewer loads in flight)
+template <bool ROLL = false>
 __device__ __forceinline__ void gather_vc(const MpmParams &P, float inv_dx, const float4 *__restrict__ gv,
                                           const Base &b, float (&nv)[3], float (&nC)[3][3]) {
   float wt[3][3];
@@ -965,18 +970,18 @@ __device__ __forceinline__ void gather_vc(const MpmParams &P, float inv_dx, cons
   float sa[3] = {0.f, 0.f, 0.f}, sb[3] = {0.f, 0.f, 0.f}, sc[3] = {0.f, 0.f, 0.f};
   nv[0] = nv[1] = nv[2] = 0.0f;
   const float wz0 = wt[0][2], wz1 = wt[1][2], wz2 = wt[2][2], wz2x2 = 2.0f * wt[2][2];
-#pragma unroll
+#pragma unroll(ROLL ? 1 : 3)
   for (int a = 0; a < 3; ++a)
 #pragma unroll
     for (int bb = 0; bb < 3; ++bb) {
-      const int line = ax[a] + ay[bb];
+      const int line = (a == 0 ? ax[0] : (a == 1 ? ax[1] : ax[2])) + ay[bb];
       const float4 g0 = __ldg(gv + line + az[0]), g1 = __ldg(gv + line + az[1]), g2 = __ldg(gv + line + az[2]);
       const float2 T01 =
           __ffma2_rn(f2(wz2, wz2), f2(g2.x, g2.y), __ffma2_rn(f2(wz1, wz1), f2(g1.x, g1.y), __fmul2_rn(f2(wz0, wz0), f2(g0.x, g0.y))));
       const float T2 = fmaf(wz2, g2.z, fmaf(wz1, g1.z, wz0 * g0.z));
       const float2 U01 = __ffma2_rn(f2(wz2x2, wz2x2), f2(g2.x, g2.y), __fmul2_rn(f2(wz1, wz1), f2(g1.x, g1.y)));
       const float U2 = fmaf(wz2x2, g2.z, wz1 * g1.z);
-      const float W = wt[a][0] * wt[bb][1];
+      const float W = (a == 0 ? wt[0][0] : (a == 1 ? wt[1][0] : wt[2][0])) * wt[bb][1];
       const float T[3] = {T01.x, T01.y, T2}, U[3] = {U01.x, U01.y, U2};
 #pragma unroll
       for (int r = 0; r < 3; ++r) {
@@ -1048,8 +1053,9 @@ __device__ __forceinline__ void flush_vmax(float *maxv_out, float vmax, int vsce
 // particles, whose stored v never changes.
 constexpr int kFusedPlain = 0, kFusedG2P2G = 1, kFusedG2P2GSorted = 2, kFusedG2P2GLast = 3;
 
-template <bool HAS_EP, int MODE, bool BATCH = false>
-__global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_fused(const MpmParams P, const MpmParams *tab,
+template <bool HAS_EP, int MODE, bool BATCH = false, bool ROLL = false>
+__global__ __launch_bounds__(kP2GThreads, ROLL ? 4 : MPM_P2G_MIN_CTAS) void k_fused(const MpmParams P,
+                                                                                   const MpmParams *tab,
                                                                           const Ws w,
                                                                           const __grid_constant__ CUtensorMap map_x,
                                                                           const __grid_constant__ CUtensorMap map_f,
@@ -1126,7 +1132,7 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_fused(const M
         // the next substep gathers them afresh and the frame's closing G2P
         // (k_g2p_stream) stores the final ones
         if (mat != 4) {
-          gather_vc(P, S.inv_dx, w.grid_vel, b0, v, C);
+          gather_vc<ROLL>(P, S.inv_dx, w.grid_vel, b0, v, C);
 #pragma unroll
           for (int d = 0; d < 3; ++d) x[d] = x[d] + dts * v[d];
         } else {  // stationary: v, C and x stay
@@ -1140,7 +1146,7 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_fused(const M
         // since then keep their v with C = 0; stationary particles gather C
         // but keep v and x
         const bool fresh = SORTED && (int64_t)(uint32_t)idword >= first_new;
-        if (!fresh) gather_vc(P, S.inv_dx, w.grid_vel, b0, v, C);
+        if (!fresh) gather_vc<ROLL>(P, S.inv_dx, w.grid_vel, b0, v, C);
         if (mat == 4 || fresh) {
 #pragma unroll
           for (int d = 0; d < 3; ++d) v[d] = st[(R::V + d) * cap + i];
@@ -1204,7 +1210,7 @@ __global__ __launch_bounds__(kP2GThreads, MPM_P2G_MIN_CTAS) void k_fused(const M
 #pragma unroll
         for (int c = 0; c < 3; ++c) adx[r][c] = cu.affine[r][c] * S.dx;
     }
-    p2g_scatter_step<true>(P, w, sm.tile, o, anchored, act, bs, wt, mass, q, adx, lane);
+    p2g_scatter_step<true, ROLL>(P, w, sm.tile, o, anchored, act, bs, wt, mass, q, adx, lane);
     g0 = g1;
   }
   if (anchored) p2g_tile_flush<true>(P, w, sm.tile, o, lane);
@@ -1616,19 +1622,19 @@ static bool rows_tensor_map(CUtensorMap *map, const float *state, int64_t cap, i
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <bool HAS_EP, bool BATCH, bool Q>
+template <bool HAS_EP, bool BATCH, bool Q, bool ROLL = BATCH>
 static int launch_p2g(int ctas, cudaStream_t s, const MpmParams &p, const MpmParams *tab, const Ws &w,
                       const float *cur, float *nxt, int64_t cap, int64_t n, float dt) {
   if (n <= 0) return MPM_OK;
   CUtensorMap map;
   if (!rows_tensor_map(&map, cur, cap, P2GRows<Q, HAS_EP>::N)) return MPM_E_CUDA;
-  k_p2g<HAS_EP, BATCH, Q><<<ctas, kP2GThreads, kP2GSmem, s>>>(p, tab, w, map, cur, nxt, cap, n, dt);
+  k_p2g<HAS_EP, BATCH, Q, ROLL><<<ctas, kP2GThreads, kP2GSmem, s>>>(p, tab, w, map, cur, nxt, cap, n, dt);
   return MPM_OK;
 }
 
-template <bool HAS_EP, bool BATCH, bool Q>
+template <bool HAS_EP, bool BATCH, bool Q, bool ROLL = BATCH>
 static int p2g_occupancy() {
-  auto k = k_p2g<HAS_EP, BATCH, Q>;
+  auto k = k_p2g<HAS_EP, BATCH, Q, ROLL>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kP2GSmem);
   int c = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&c, k, kP2GThreads, kP2GSmem);
@@ -1648,16 +1654,19 @@ struct DevInfo {
   int p2g_q_ctas = 0, p2g_ep_q_ctas = 0, g2p_q_ctas = 0, g2p2g_q_ctas = 0;  // packed storage
   int fused_ctas[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};  // k_fused [has_Ep][mode]
   int fused_b_ctas[2] = {0, 0};                    // batched k_fused [has_Ep]
+  int fused_roll_ctas[2][2] = {{0, 0}, {0, 0}};    // rolled k_fused [has_Ep][plain, G2P2G in place]
+  int p2g_roll_ctas[2] = {0, 0};                   // rolled k_p2g [has_Ep]
   int g2ps_ctas = 0, g2ps_b_ctas = 0, binbox_ctas = 0;
 };
 
 // CTAs of one full wave of k_fused<HAS_EP, MODE, BATCH> (its dynamic shared
 // memory opted in first)
-template <bool HAS_EP, int MODE, bool BATCH = false>
+template <bool HAS_EP, int MODE, bool BATCH = false, bool ROLL = false>
 static void fused_occupancy(int sms, int &ctas) {
   int k = 0;
-  cudaFuncSetAttribute(k_fused<HAS_EP, MODE, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFusedSmem);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, k_fused<HAS_EP, MODE, BATCH>, kP2GThreads, kFusedSmem);
+  auto kern = k_fused<HAS_EP, MODE, BATCH, ROLL>;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFusedSmem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k, kern, kP2GThreads, kFusedSmem);
   ctas = sms * (k > 0 ? k : 1);
 }
 
@@ -1707,6 +1716,12 @@ static const DevInfo *dev_info() {
       fused_occupancy<true, kFusedG2P2GLast>(sms, d.fused_ctas[1][3]);
       fused_occupancy<false, kFusedPlain, true>(sms, d.fused_b_ctas[0]);
       fused_occupancy<true, kFusedPlain, true>(sms, d.fused_b_ctas[1]);
+      fused_occupancy<false, kFusedPlain, false, true>(sms, d.fused_roll_ctas[0][0]);
+      fused_occupancy<true, kFusedPlain, false, true>(sms, d.fused_roll_ctas[1][0]);
+      fused_occupancy<false, kFusedG2P2G, false, true>(sms, d.fused_roll_ctas[0][1]);
+      fused_occupancy<true, kFusedG2P2G, false, true>(sms, d.fused_roll_ctas[1][1]);
+      d.p2g_roll_ctas[0] = sms * p2g_occupancy<false, false, false, true>();
+      d.p2g_roll_ctas[1] = sms * p2g_occupancy<true, false, false, true>();
       int gs = 0, gsb = 0, bb = 0;
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&gs, k_g2p_stream<false>, 128, 0);
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&gsb, k_g2p_stream<true>, 128, 0);
@@ -1726,6 +1741,10 @@ static int launch_p2g_single(const DevInfo *di, cudaStream_t s, const MpmParams 
   if (p.quant)
     return p.has_Ep ? launch_p2g<true, false, true>(di->p2g_ep_q_ctas, s, p, nullptr, w, cur, nxt, cap, n, dt)
                     : launch_p2g<false, false, true>(di->p2g_q_ctas, s, p, nullptr, w, cur, nxt, cap, n, dt);
+  if (p.occupancy)  // rolled, 16 warps per SM
+    return p.has_Ep ? launch_p2g<true, false, false, true>(di->p2g_roll_ctas[1], s, p, nullptr, w, cur, nxt, cap, n, dt)
+                    : launch_p2g<false, false, false, true>(di->p2g_roll_ctas[0], s, p, nullptr, w, cur, nxt, cap, n,
+                                                            dt);
   return p.has_Ep ? launch_p2g<true, false, false>(di->p2g_ep_ctas, s, p, nullptr, w, cur, nxt, cap, n, dt)
                   : launch_p2g<false, false, false>(di->p2g_ctas, s, p, nullptr, w, cur, nxt, cap, n, dt);
 }
@@ -1936,7 +1955,20 @@ static int fused_particles(const DevInfo *di, cudaStream_t s, const MpmParams &p
   const int nf = p.has_Ep ? kFusedRowsF : (MODE == kFusedG2P2GSorted ? kFusedRowsF - 1 : kFusedRowsF - 2);
   if (!rows_tensor_map(&mx, st, cap, MPM_NROWS, 3) || !rows_tensor_map(&mf, st, cap, MPM_NROWS, nf))
     return MPM_E_CUDA;
-  const int ctas = BATCH ? di->fused_b_ctas[p.has_Ep ? 1 : 0] : di->fused_ctas[p.has_Ep ? 1 : 0][MODE];
+  const int ep = p.has_Ep ? 1 : 0;
+  if constexpr (!BATCH && (MODE == kFusedPlain || MODE == kFusedG2P2G)) {
+    if (p.occupancy) {  // rolled, 16 warps per SM
+      constexpr int R = MODE == kFusedPlain ? 0 : 1;
+      if (p.has_Ep)
+        k_fused<true, MODE, false, true><<<di->fused_roll_ctas[1][R], kP2GThreads, kFusedSmem, s>>>(
+            p, tab, w, mx, mf, st, out, cap, n, dt, first_new, maxv);
+      else
+        k_fused<false, MODE, false, true><<<di->fused_roll_ctas[0][R], kP2GThreads, kFusedSmem, s>>>(
+            p, tab, w, mx, mf, st, out, cap, n, dt, first_new, maxv);
+      return MPM_OK;
+    }
+  }
+  const int ctas = BATCH ? di->fused_b_ctas[ep] : di->fused_ctas[ep][MODE];
   if (p.has_Ep)
     k_fused<true, MODE, BATCH><<<ctas, kP2GThreads, kFusedSmem, s>>>(p, tab, w, mx, mf, st, out, cap, n, dt,
                                                                     first_new, maxv);

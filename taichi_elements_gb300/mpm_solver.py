@@ -220,6 +220,10 @@ class MPMSolver:
         # positions in between); autotune.tune_schedule measures both choices
         self.fuse_frames = True
         self.resort_every = 24
+        # MpmParams.occupancy: 0 = the fused and P2G kernels' stencil loops
+        # fully unrolled at 12 warps per SM, 1 = rolled at 16 (the faster one
+        # depends on the scene; autotune.tune_schedule measures both)
+        self._occupancy = 0
         self.chunk = int(chunk) if chunk else self.DEFAULT_CHUNK
         self.use_cuda_graph = use_cuda_graph
         self.autotune = bool(autotune)
@@ -290,6 +294,7 @@ class MPMSolver:
         p.chunk = self.chunk
         p.plasticity = int(bool(self.support_plasticity))
         p.quant = int(bool(self.quant))
+        p.occupancy = self._occupancy
         p.dx = self.dx
         p.inv_dx = self.inv_dx
         p.p_vol = self.p_vol
@@ -326,6 +331,18 @@ class MPMSolver:
             self._params_version += 1
             self._graphs.clear()
         return self._params
+
+    @property
+    def occupancy(self) -> int:
+        """Register budget of the fused and P2G kernels (MpmParams.occupancy)."""
+        return self._occupancy
+
+    @occupancy.setter
+    def occupancy(self, value):
+        value = int(bool(value))
+        if value != self._occupancy:
+            self._occupancy = value
+            self._invalidate_params()
 
     def _invalidate_params(self):
         self._params = None

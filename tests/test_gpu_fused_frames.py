@@ -68,3 +68,21 @@ def test_fused_frames_graph_replay_matches_eager():
     torch.cuda.synchronize()
     xa, xb = a.particle_info()["position"], b.particle_info()["position"]
     assert np.abs(xa - xb).max() < 1e-5
+
+
+@pytest.mark.parametrize("fuse", [True, False])
+def test_rolled_kernels_match_oracle(fuse):
+    """MpmParams.occupancy = 1 (the fused and P2G kernels' stencil x loops
+    rolled, 16 warps per SM): a fused frame, and the per-substep launches,
+    against the float64 oracle as above."""
+    sc = scenes.four_materials_128(per_cube=20000)
+    s = sc.make_solver()
+    s.occupancy = 1
+    s.fuse_frames = fuse
+    s.resort_every = 3
+    frame_dt = 20 * sc.default_dt * 0.999
+    count, dt = s.count_substeps(frame_dt, sc.default_dt)
+    s.step(frame_dt)
+    P64, P32 = _oracle_frame(sc, count, dt)
+    assert_bounds(f"{sc.name}, rolled kernels, {'fused frame' if fuse else 'per-substep'} of {count} substeps",
+                  _errors(s, P64, P32), f32_calibrated=True)

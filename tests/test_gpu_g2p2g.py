@@ -207,3 +207,18 @@ def test_g2p2g_frame_after_particles_were_added():
     g = gpu_particles(s)
     assert rel_inf(g['x'], R.P.x, 1.0) < 1e-5
     assert rel_inf(g['v'], R.P.v, max(np.abs(R.P.v).max(), 1e-3)) < 1e-4
+
+
+def test_g2p2g_frames_rolled_match_oracle():
+    """The G2P2G frames with MpmParams.occupancy = 1 (rolled stencil loops)."""
+    sc = scenes.four_materials_128(per_cube=8000)
+    s, R64, R32, win = start(sc)
+    s.occupancy = 1
+    s.resort_every = 3
+    count, dt = s.count_substeps(20 * sc.default_dt * 0.999, sc.default_dt)
+    s.step(20 * sc.default_dt * 0.999)
+    for _ in range(count):
+        R64.step(dt)
+        R32.step(dt)
+    assert_bounds(f"{sc.name} G2P2G frame of {count} substeps, rolled kernels", errors(s, R64, R32, win),
+                  f32_calibrated=True)

@@ -312,7 +312,9 @@ def test_schedule_autotune_applies_a_measured_choice_and_leaves_state_untouched(
     choice = tune_schedule(s)
     assert choice["mode"] in ("frame", "substep") and choice["chunk"] in CANDIDATES
     assert set(map(int, choice["frame_ms"])) == set(RESORT_CANDIDATES)
+    assert set(map(int, choice["frame_ms_rolled"])) == set(RESORT_CANDIDATES)
     assert s.fuse_frames == (choice["mode"] == "frame") and s.chunk == choice["chunk"]
+    assert s.occupancy == choice["occupancy"]
     if s.fuse_frames:
         assert s.resort_every == choice["resort"]
     assert torch.equal(s.full_state()['x'], before)

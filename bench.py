@@ -311,13 +311,15 @@ def run_gb300(args):
     solver.use_cuda_graph = False  # events between launches; the graph replays the same kernels
     dt = sc.default_dt
     tuned = None
-    if args.chunk is None and args.resort is None and args.schedule is None:
+    if args.chunk is None and args.resort is None and args.schedule is None and args.occupancy is None:
         from taichi_elements_gb300.autotune import tune_schedule
         tuned = tune_schedule(solver)
     if args.resort is not None:
         solver.resort_every = args.resort
     if args.schedule is not None:
         solver.fuse_frames = args.schedule == "frame"
+    if args.occupancy is not None:
+        solver.occupancy = args.occupancy
     fused = solver._fuses_frames
     lib = solver._lib
     stream = torch.cuda.current_stream()
@@ -395,6 +397,7 @@ def run_gb300(args):
                         "k_g2p_stream": G2P_BYTES_PER_PARTICLE * n + G2P_BYTES_PER_NODE * n_nodes}
         top = max(kernel_bytes, key=lambda k: totals[k])
         schedule = {"mode": "fused frames (mpm_frame)", "resort_every": solver.resort_every,
+                    "occupancy": solver.occupancy,
                     "resort_per_frame": resorts,
                     "frames": plan, "launches_per_kernel": {k: len(v) for k, v in kt.items()},
                     "ms_per_launch": per_launch}
@@ -1002,6 +1005,8 @@ def main():
     ap.add_argument("--frame", type=int, default=50, help="substeps per mpm_frame call in the timed region")
     ap.add_argument("--schedule", choices=["frame", "substep"], default=None,
                     help="fused frames or per-substep launches (default: the autotuner's choice)")
+    ap.add_argument("--occupancy", type=int, choices=[0, 1], default=None,
+                    help="fused/P2G kernels unrolled at 12 warps per SM (0) or rolled at 16 (1)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")

@@ -36,6 +36,7 @@ import ctypes
 import math
 import numbers
 import sys
+import threading
 import time
 
 import numpy as np
@@ -74,11 +75,16 @@ class ParticleCount(int):
 # Unused pairs are dropped, oldest first, above _PINNED_POOL_BYTES.
 _pinned_pool: list = []
 _PINNED_POOL_BYTES = 8 << 30
+_pinned_lock = threading.Lock()
 
 
 def _pinned_buffer(shape, dtype):
     """A free (pinned tensor, numpy view) pair of this shape and dtype."""
-    shape = tuple(shape)
+    with _pinned_lock:
+        return _pinned_buffer_locked(tuple(shape), dtype)
+
+
+def _pinned_buffer_locked(shape, dtype):
     for pair in _pinned_pool:
         h, hn = pair
         # held by the pool alone: the pair, the local name, getrefcount's argument

@@ -240,15 +240,11 @@ def time_frames(solver, dt, plan, stream):
     Returns the events per frame (synchronised)."""
     import torch
 
-    from taichi_elements_gb300 import _lib
-    evs = []
-    for c in plan:
-        fe = [torch.cuda.Event(enable_timing=True) for _ in range(5 * c + 2)]
-        for e in fe:
-            e.record(stream)  # creates the event
-        evs.append(fe)
+    from taichi_elements_gb300 import _lib, profiler
+    with torch.cuda.stream(stream):
+        made = [profiler.frame_events(c) for c in plan]
+    evs, arrays = [m[0] for m in made], [m[1] for m in made]
     torch.cuda.synchronize()
-    arrays = [(ctypes.c_void_p * len(fe))(*[e.cuda_event for e in fe]) for fe in evs]
     if max(plan) > solver._maxv.numel():
         solver._maxv = torch.zeros(max(plan), dtype=torch.float32, device=solver.device)
     p = solver.params
@@ -274,28 +270,14 @@ def time_frames(solver, dt, plan, stream):
 
 
 def frame_kernel_times(plan, evs, resorts, g2p2g=False):
-    """Per launch group durations (ms) from the events of time_frames.  Plain
-    frames: the sort's P2G (k_p2g), the fused substeps (k_fused), the closing
-    G2P that also bins (k_g2p_stream); G2P2G frames: the sorting pass
-    (k_fused_sorted), the in-place substeps (k_fused) and the binning passes
-    (k_bin_box).  "binning" is the sorts' finalize, "grid" the grid update
-    with the flag passes.  `resorts`: each frame's re-sort interval."""
-    sort_k, bin_k = ("k_fused_sorted", "k_bin_box") if g2p2g else ("k_p2g", "k_g2p_stream")
-    out = {sort_k: [], "k_fused": [], bin_k: [], "binning": [], "grid": []}
+    """Per launch group durations (ms) over the frames of time_frames (the
+    decoding of taichi_elements_gb300.profiler.frame_kernel_times, frame by
+    frame).  `resorts`: each frame's re-sort interval."""
+    from taichi_elements_gb300.profiler import frame_kernel_times as one_frame
+    out = {}
     for c, ev, resort in zip(plan, evs, resorts):
-        def t(i, j):
-            return ev[i].elapsed_time(ev[j])
-        for k in range(c):
-            b = 5 * k
-            if k % resort == 0:
-                if k > 0:
-                    out[bin_k].append(t(b, b + 1))
-                out["binning"].append(t(b + 1, b + 2))
-                out[sort_k].append(t(b + 2, b + 3))
-            else:
-                out["k_fused"].append(t(b + 2, b + 3))
-            out["grid"].append(t(b + 3, b + 4))
-        out[bin_k].append(t(5 * c, 5 * c + 1))
+        for k, v in one_frame(c, ev, resort, g2p2g).items():
+            out.setdefault(k, []).extend(v)
     return out
 
 

@@ -18,7 +18,7 @@ import math
 import numpy as np
 import torch
 
-from . import _lib
+from . import _lib, profiler
 from .mpm_solver import frame_resort_interval
 from ._lib import KIND_BOX, KIND_SURFACE, NROWS, ROW_C, ROW_F, ROW_ID, ROW_JP, ROW_MAT, ROW_V, ROW_X
 
@@ -215,20 +215,30 @@ class BatchedMPM:
         cur = self._state[self._cur]
         nxt = self._state[1 - self._cur]
         mv = self._maxv[slot].data_ptr() if slot >= 0 else None
+        if profiler.kernel_profiler:
+            e0, e1 = profiler.substep_events()
+            e0.record(torch.cuda.current_stream(self.device))
         _lib.check(self._lib.mpm_batch_substep(ctypes.byref(self._header), self._rows.data_ptr(), self._ws.data_ptr(),
                                                self.cap, self.n_particles, cur.data_ptr(), nxt.data_ptr(), mv,
                                                self.stream), "mpm_batch_substep")
+        if profiler.kernel_profiler:
+            e1.record(torch.cuda.current_stream(self.device))
+            profiler.add_call("mpm_batch_substep", e0, e1)
         self._cur = 1 - self._cur
 
     def _launch_frame(self, count: int):
         """All `count` substeps as one fused frame (mpm_batch_frame)."""
         in_b = ctypes.c_int32(0)
+        resort = frame_resort_interval(count, self.resort_every)
+        evs, arr = profiler.frame_events(count) if profiler.kernel_profiler else (None, None)
         _lib.check(self._lib.mpm_batch_frame(ctypes.byref(self._header), self._rows.data_ptr(), self._ws.data_ptr(),
                                              self.cap, self.n_particles, self._state[self._cur].data_ptr(),
                                              self._state[1 - self._cur].data_ptr(), int(count),
-                                             frame_resort_interval(count, self.resort_every), self._maxv.data_ptr(),
-                                             ctypes.byref(in_b), None, self.stream), "mpm_batch_frame")
+                                             resort, self._maxv.data_ptr(), ctypes.byref(in_b), arr, self.stream),
+                   "mpm_batch_frame")
         self._cur = (self._cur + int(in_b.value)) % 2
+        if evs is not None:
+            profiler.add_frame(count, evs, resort, prefix="batch ")
 
     def _launch_all(self, count: int):
         self._maxv[:count].zero_()
@@ -247,7 +257,9 @@ class BatchedMPM:
             self._maxv = torch.zeros((count, len(self.scenes)), dtype=torch.float32, device=self.device)
         key = (count, self._cur, self.fuse_frames, self.resort_every)
         g = self._graphs.get(key)
-        if self.use_cuda_graph and g is None and key in self._seen:
+        if profiler.kernel_profiler:  # events need the launches themselves
+            g = None
+        elif self.use_cuda_graph and g is None and key in self._seen:
             start = self._cur
             g = torch.cuda.CUDAGraph()
             with torch.cuda.graph(g):

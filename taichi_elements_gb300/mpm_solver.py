@@ -42,7 +42,7 @@ import time
 import numpy as np
 import torch
 
-from . import _lib
+from . import _lib, profiler
 from ._lib import (KIND_BOX, KIND_SPHERE, KIND_SURFACE, NROWS, QROWS, ROW_C, ROW_EP, ROW_F, ROW_ID, ROW_JP, ROW_MAT,
                    ROW_V, ROW_X)
 
@@ -760,6 +760,17 @@ class MPMSolver:
         cur = self._state[self._cur]
         nxt = self._state[1 - self._cur]
         mv = _ptr(self._maxv) + 4 * maxv_slot if maxv_slot >= 0 else None
+        if profiler.kernel_profiler:
+            e0, e1 = profiler.substep_events()
+            e0.record(torch.cuda.current_stream(self.device))
+            self._launch_substep_call(dt, p, cur, nxt, mv)
+            e1.record(torch.cuda.current_stream(self.device))
+            name = "mpm_g2p2g_substep" if self.use_g2p2g else ("mpm_substep (quant)" if self.quant else "mpm_substep")
+            profiler.add_call(name, e0, e1)
+        else:
+            self._launch_substep_call(dt, p, cur, nxt, mv)
+
+    def _launch_substep_call(self, dt, p, cur, nxt, mv):
         if self.use_g2p2g:
             first_new = self._last_final if self._g2p2g_grid_valid else 0
             _lib.check(
@@ -823,6 +834,7 @@ class MPMSolver:
         the G2P2G mode's substeps."""
         p = self.params
         in_b = ctypes.c_int32(0)
+        evs, arr = profiler.frame_events(count) if profiler.kernel_profiler else (None, None)
         if self.use_g2p2g:
             if self._g2p2g_listed:  # per-substep calls left finalized lists: count afresh
                 _lib.check(self._lib.mpm_bin_count(ctypes.byref(p), _ptr(self._ws), self._cap,
@@ -833,7 +845,7 @@ class MPMSolver:
                 self._lib.mpm_g2p2g_frame(ctypes.byref(p), _ptr(self._ws), self._cap, self.n_particles,
                                           _ptr(self._state[self._cur]), _ptr(self._state[1 - self._cur]), float(dt),
                                           int(count), int(self._frame_resort(count)), int(first_new),
-                                          _ptr(self._maxv), ctypes.byref(in_b), None, self.stream), "mpm_g2p2g_frame")
+                                          _ptr(self._maxv), ctypes.byref(in_b), arr, self.stream), "mpm_g2p2g_frame")
             # the state is binned (counts) for the next frame or substep
             self._g2p2g_listed = 0
             self._binned = self.n_particles
@@ -843,9 +855,11 @@ class MPMSolver:
             _lib.check(
                 self._lib.mpm_frame(ctypes.byref(p), _ptr(self._ws), self._cap, self.n_particles,
                                     _ptr(self._state[self._cur]), _ptr(self._state[1 - self._cur]), float(dt),
-                                    int(count), int(self._frame_resort(count)), _ptr(self._maxv), ctypes.byref(in_b), None,
+                                    int(count), int(self._frame_resort(count)), _ptr(self._maxv), ctypes.byref(in_b), arr,
                                     self.stream), "mpm_frame")
         self._cur = (self._cur + int(in_b.value)) % 2
+        if evs is not None:
+            profiler.add_frame(count, evs, self._frame_resort(count), g2p2g=self.use_g2p2g)
 
     def _frame_resort(self, count: int) -> int:
         """The re-sort interval of a fused frame of `count` substeps: the
@@ -874,7 +888,7 @@ class MPMSolver:
                self._fuses_frames, self.resort_every)
         if self.use_g2p2g:  # the first substep's launch depends on the mode's state
             key += (bool(self._g2p2g_listed), self._last_final if self._g2p2g_grid_valid else 0)
-        if not self.use_cuda_graph:
+        if not self.use_cuda_graph or profiler.kernel_profiler:  # events need the launches themselves
             self._launch_substeps(count, dt)
             return
         g = self._graphs.get(key)
@@ -924,6 +938,8 @@ class MPMSolver:
         else:
             maxv = np.zeros(count, dtype=np.float32)
             dts = [dt] * count
+        if profiler.kernel_profiler:
+            profiler.collect(sync=False)  # the frame's readback synchronised the stream
         for s in range(count):
             self.total_substeps += 1
             self.t += dts[s]
@@ -933,11 +949,27 @@ class MPMSolver:
         if count:
             self.all_time_max_velocity = max(self.all_time_max_velocity, float(maxv.max()))
         if print_stat:
+            profiler.print_kernel_profiler_info()
+            profiler.print_memory_profiler_info(self)
             cur_frame_velocity = float(maxv[-1]) if count else 0.0
             print(f'CFL: {cur_frame_velocity * dt / self.dx}')
             print(f'num particles={self.n_particles}')
             print(f'  frame time {time.time() - begin_t:.3f} s')
             print(f'  substep time {1000 * (time.time() - begin_t) / max(1, self.total_substeps - begin_substep):.3f} ms')
+
+    def memory_report(self) -> list:
+        """(name, bytes) of the device buffers this solver holds."""
+        rows = []
+        if self._state[0] is not None:
+            r, cap = self._state[0].shape
+            rows.append((f"particle state: 2 buffers x {r} rows x {cap} slots (float32"
+                         f"{', packed' if self.quant else ''})", 2 * self._state[0].numel() * 4))
+            rows.append(("particle colours and emitter ids", (self._color.numel() + self._emitter.numel()) * 4))
+        if self._ws is not None:
+            rows.append(("workspace: grid momentum / velocity window, block flags and lists, cell counters, "
+                         "sort tables, status", self._ws.numel()))
+        rows.append(("max |v| per substep", self._maxv.numel() * 4))
+        return rows
 
     def _max_grid_velocity(self) -> float:
         """compute_max_grid_velocity (engine/mpm_solver.py:737-746) of the

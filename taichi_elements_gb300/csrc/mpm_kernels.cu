@@ -1066,6 +1066,11 @@ __global__ __launch_bounds__(kP2GThreads, ROLL ? 4 : MPM_P2G_MIN_CTAS) void k_fu
   using R = PRows<false>;
   constexpr bool G2P2G = MODE != kFusedPlain;
   constexpr bool SORTED = MODE == kFusedG2P2GSorted;
+  // ROLL rolls the scatter's x loop (4 CTAs, 16 warps per SM).  The plain
+  // mode without per-particle E keeps its gather unrolled within that budget
+  // (8 B of spills; 16M / 2M scenes: 1.445 / 0.320 ms per launch against
+  // 1.540 / 0.323 with both loops rolled); the other modes roll both.
+  constexpr bool ROLL_GATHER = ROLL && (G2P2G || HAS_EP);
   static_assert(!(BATCH && G2P2G), "the batched form runs the plain loop");
   // staged rows from F on: F, Jp, material[, id][, E].  Only the sorted pass
   // needs the id: particles added since the last substep (id >= first_new)
@@ -1132,7 +1137,7 @@ __global__ __launch_bounds__(kP2GThreads, ROLL ? 4 : MPM_P2G_MIN_CTAS) void k_fu
         // the next substep gathers them afresh and the frame's closing G2P
         // (k_g2p_stream) stores the final ones
         if (mat != 4) {
-          gather_vc<ROLL>(P, S.inv_dx, w.grid_vel, b0, v, C);
+          gather_vc<ROLL_GATHER>(P, S.inv_dx, w.grid_vel, b0, v, C);
 #pragma unroll
           for (int d = 0; d < 3; ++d) x[d] = x[d] + dts * v[d];
         } else {  // stationary: v, C and x stay
@@ -1146,7 +1151,7 @@ __global__ __launch_bounds__(kP2GThreads, ROLL ? 4 : MPM_P2G_MIN_CTAS) void k_fu
         // since then keep their v with C = 0; stationary particles gather C
         // but keep v and x
         const bool fresh = SORTED && (int64_t)(uint32_t)idword >= first_new;
-        if (!fresh) gather_vc<ROLL>(P, S.inv_dx, w.grid_vel, b0, v, C);
+        if (!fresh) gather_vc<ROLL_GATHER>(P, S.inv_dx, w.grid_vel, b0, v, C);
         if (mat == 4 || fresh) {
 #pragma unroll
           for (int d = 0; d < 3; ++d) v[d] = st[(R::V + d) * cap + i];

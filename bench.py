@@ -797,39 +797,37 @@ def run_render_measure(solver, with_cpu, spp=8):
 def run_batched_measure(frames=3, substeps=50):
     """64 independent scenes (grids 32-96^3, 8K-300K particles each) advanced
     by the batched engine in CUDA-graph frames of `substeps` substeps (its
-    default per-substep launches, then the same frames fused), and the same
-    scenes advanced by the plain solver looped scene by scene."""
+    default per-substep launches, then the same frames fused at both register
+    budgets, each from the initial state), and the same scenes advanced by
+    the plain solver looped scene by scene."""
     import torch
 
     from taichi_elements_gb300 import scenes
     from taichi_elements_gb300.batched import BatchedMPM, BatchScene
     raw = scenes.batched_scenes()
     total = sum(s.n for s in raw)
-    B = BatchedMPM([BatchScene.from_scene(s) for s in raw])
     stream = torch.cuda.current_stream()
-    for _ in range(2):
-        B.substeps(substeps)  # first run, then graph capture
-    torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(frames):
-        B.substeps(substeps)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    B.check_status()
-    t_b = e0.elapsed_time(e1) / 1e3
-    B.fuse_frames = True  # the same frames as fused frames (mpm_batch_frame)
-    for _ in range(2):
-        B.substeps(substeps)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(frames):
-        B.substeps(substeps)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    B.check_status()
-    t_bs = e0.elapsed_time(e1) / 1e3
-    del B
+
+    def timed(fuse_frames, occupancy=0):
+        """Frames from the scenes' initial state: per-substep launches, or
+        fused frames (mpm_batch_frame) with the fused kernel's budget."""
+        B = BatchedMPM([BatchScene.from_scene(s) for s in raw])
+        B.fuse_frames, B.occupancy = fuse_frames, occupancy
+        for _ in range(2):
+            B.substeps(substeps)  # first run, then graph capture
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(frames):
+            B.substeps(substeps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        B.check_status()
+        return e0.elapsed_time(e1) / 1e3
+
+    t_b = timed(False)
+    t_bs = timed(True)
+    t_bs16 = timed(True, 1)
     solvers = [s.make_solver() for s in raw]
     for sv, s in zip(solvers, raw):
         sv._prepare(s.default_dt)
@@ -847,6 +845,7 @@ def run_batched_measure(frames=3, substeps=50):
     v_l = total * substeps * frames / t_l
     return {"value": v_b, "unit": "particle-substeps/s", "looped_plain_value": v_l, "speedup_vs_looped": v_b / v_l,
             "fused_frames_value": total * substeps * frames / t_bs,
+            "fused_frames_16warps_value": total * substeps * frames / t_bs16,
             "scenes": len(raw), "particles": total, "substeps_per_frame": substeps, "frames": frames,
             "workload": "64 scenes, grids {32,48,64,96}^3, 8K-300K particles in 1-3 cubes, 4 materials, "
                         "per-scene E log-uniform 1e4-1e6, CUDA-graph 50-substep frames"}

@@ -101,10 +101,13 @@ typedef struct MpmParams {
                        * holds the packed 21-row layout (MPM_QROWS) */
   int32_t occupancy;  /* register budget of the fused and streaming P2G
                        * kernels: 0 = stencil loops fully unrolled, 3 CTAs
-                       * (12 warps) per SM; 1 = their x loops rolled, 4 CTAs
-                       * (16 warps) per SM.  Results are the same; which is
+                       * (12 warps) per SM; 1 = 4 CTAs (16 warps) per SM, the
+                       * scatter's x loop rolled (and the gather's, except in
+                       * the plain loop's single-scene fused kernel without
+                       * per-particle E).  Results are the same; which is
                        * faster depends on the scene (measured per scene by
-                       * the Python autotuner) */
+                       * the Python autotuner).  In a batch header it selects
+                       * the budget of mpm_batch_frame's fused kernel */
   float dx, inv_dx, p_vol, p_mass;
   float mu0, la0, nu, alpha; /* Lame parameters, Poisson ratio, sand alpha */
   float water_density;
@@ -439,6 +442,16 @@ int mpm_render_first_hits(const void *scene, const uint32_t *occ, const int64_t 
  * the grid-active blocks of the last substep (0 before the first).  Used by
  * the adaptive time step (use_adaptive_dt, :761-766). */
 int mpm_max_grid_velocity(const MpmParams *p, void *ws, int64_t cap, float *out, void *stream);
+
+/* The constitutive update of P2G (engine/mpm_solver.py:506-574, with
+ * sand_projection :321-342) for n independent particles, by the device code
+ * the P2G kernels run: material[i] (0-4), F[9 i .. 9 i + 8] (row major) and
+ * Jp[i] updated in place, C[9 i ..] read, affine[9 i ..] written with the
+ * APIC matrix -dt p_vol 4 inv_dx^2 stress + mass C (:569-574).  A diagnostic
+ * entry point for tests on chosen deformation gradients (inverted, nearly
+ * singular, clamped); device pointers; single-scene parameters. */
+int mpm_constitutive_eval(const MpmParams *p, int64_t n, const int32_t *material, float *F, const float *C,
+                          float *Jp, float *affine, float dt, void *stream);
 
 /* Pointer to the device status word inside the workspace (uint32). */
 int mpm_status_ptr(const MpmParams *p, void *ws, int64_t cap, uint32_t **status_out);

@@ -141,6 +141,7 @@ SIGNATURES = {
     "mpm_quant_unpack": [_v, _i64, _i64, _i64, _v, _i64, _v],
     "mpm_status_ptr": [_P, _v, _i64, ctypes.POINTER(ctypes.c_void_p)],
     "mpm_max_grid_velocity": [_P, _v, _i64, _v, _v],
+    "mpm_constitutive_eval": [_P, _i64, _v, _v, _v, _v, _v, _f, _v],
     "mpm_views": [_P, _v, _i64, ctypes.POINTER(MpmViews)],
 }
 

@@ -133,6 +133,17 @@ class BatchedMPM:
         self.resort_every = 24
 
     @property
+    def occupancy(self) -> int:
+        """Register budget of the fused frames' particle kernel (0: 12 warps
+        per SM, stencil loops unrolled; 1: 16 warps per SM, x loops rolled)."""
+        return int(self._header.occupancy)
+
+    @occupancy.setter
+    def occupancy(self, value: int):
+        self._header.occupancy = int(bool(value))
+        self._graphs.clear()
+
+    @property
     def stream(self) -> int:
         return torch.cuda.current_stream(self.device).cuda_stream
 
@@ -255,7 +266,7 @@ class BatchedMPM:
             return
         if self._maxv.shape[0] < count:
             self._maxv = torch.zeros((count, len(self.scenes)), dtype=torch.float32, device=self.device)
-        key = (count, self._cur, self.fuse_frames, self.resort_every)
+        key = (count, self._cur, self.fuse_frames, self.resort_every, self.occupancy)
         g = self._graphs.get(key)
         if profiler.kernel_profiler:  # events need the launches themselves
             g = None

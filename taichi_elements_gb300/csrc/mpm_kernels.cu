@@ -1069,8 +1069,9 @@ __global__ __launch_bounds__(kP2GThreads, ROLL ? 4 : MPM_P2G_MIN_CTAS) void k_fu
   // ROLL rolls the scatter's x loop (4 CTAs, 16 warps per SM).  The plain
   // mode without per-particle E keeps its gather unrolled within that budget
   // (8 B of spills; 16M / 2M scenes: 1.445 / 0.320 ms per launch against
-  // 1.540 / 0.323 with both loops rolled); the other modes roll both.
-  constexpr bool ROLL_GATHER = ROLL && (G2P2G || HAS_EP);
+  // 1.540 / 0.323 with both loops rolled); the other modes and the batched
+  // form roll both (they would spill 24-66 B).
+  constexpr bool ROLL_GATHER = ROLL && (G2P2G || HAS_EP || BATCH);
   static_assert(!(BATCH && G2P2G), "the batched form runs the plain loop");
   // staged rows from F on: F, Jp, material[, id][, E].  Only the sorted pass
   // needs the id: particles added since the last substep (id >= first_new)
@@ -1581,6 +1582,30 @@ __global__ __launch_bounds__(256) void k_max_grid_velocity(const MpmParams P, co
   if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax((int *)out, __float_as_int(m));
 }
 
+// The constitutive update of P2G for n independent particles (the diagnostic
+// entry mpm_constitutive_eval): F (row major), Jp updated in place, the APIC
+// affine matrix written, by the same device code the P2G kernels run.
+__global__ void k_constitutive_eval(const MpmParams P, int64_t n, const int32_t *__restrict__ material,
+                                    float *__restrict__ F, const float *__restrict__ C, float *__restrict__ Jp,
+                                    float *__restrict__ affine, float dt) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float f[3][3], c[3][3];
+#pragma unroll
+  for (int a = 0; a < 9; ++a) {
+    f[a / 3][a % 3] = F[9 * i + a];
+    c[a / 3][a % 3] = C[9 * i + a];
+  }
+  float jp = Jp[i];
+  const P2GOut o = constitutive<false, false>(P, dt, material[i] & 0xFF, 0.0f, f, jp, c);
+#pragma unroll
+  for (int a = 0; a < 9; ++a) {
+    F[9 * i + a] = f[a / 3][a % 3];
+    affine[9 * i + a] = o.affine[a / 3][a % 3];
+  }
+  Jp[i] = jp;
+}
+
 __global__ void k_gather_rows(const float *__restrict__ ps, int64_t cap, int64_t n, int row0, int ncols,
                               float *__restrict__ out) {
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1659,6 +1684,7 @@ struct DevInfo {
   int p2g_q_ctas = 0, p2g_ep_q_ctas = 0, g2p_q_ctas = 0, g2p2g_q_ctas = 0;  // packed storage
   int fused_ctas[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};  // k_fused [has_Ep][mode]
   int fused_b_ctas[2] = {0, 0};                    // batched k_fused [has_Ep]
+  int fused_b_roll_ctas[2] = {0, 0};               // batched rolled k_fused [has_Ep]
   int fused_roll_ctas[2][2] = {{0, 0}, {0, 0}};    // rolled k_fused [has_Ep][plain, G2P2G in place]
   int p2g_roll_ctas[2] = {0, 0};                   // rolled k_p2g [has_Ep]
   int g2ps_ctas = 0, g2ps_b_ctas = 0, binbox_ctas = 0;
@@ -1725,6 +1751,8 @@ static const DevInfo *dev_info() {
       fused_occupancy<true, kFusedPlain, false, true>(sms, d.fused_roll_ctas[1][0]);
       fused_occupancy<false, kFusedG2P2G, false, true>(sms, d.fused_roll_ctas[0][1]);
       fused_occupancy<true, kFusedG2P2G, false, true>(sms, d.fused_roll_ctas[1][1]);
+      fused_occupancy<false, kFusedPlain, true, true>(sms, d.fused_b_roll_ctas[0]);
+      fused_occupancy<true, kFusedPlain, true, true>(sms, d.fused_b_roll_ctas[1]);
       d.p2g_roll_ctas[0] = sms * p2g_occupancy<false, false, false, true>();
       d.p2g_roll_ctas[1] = sms * p2g_occupancy<true, false, false, true>();
       int gs = 0, gsb = 0, bb = 0;
@@ -1973,6 +2001,17 @@ static int fused_particles(const DevInfo *di, cudaStream_t s, const MpmParams &p
       return MPM_OK;
     }
   }
+  if constexpr (BATCH && MODE == kFusedPlain) {
+    if (p.occupancy) {  // rolled, 16 warps per SM
+      if (p.has_Ep)
+        k_fused<true, MODE, true, true><<<di->fused_b_roll_ctas[1], kP2GThreads, kFusedSmem, s>>>(
+            p, tab, w, mx, mf, st, out, cap, n, dt, first_new, maxv);
+      else
+        k_fused<false, MODE, true, true><<<di->fused_b_roll_ctas[0], kP2GThreads, kFusedSmem, s>>>(
+            p, tab, w, mx, mf, st, out, cap, n, dt, first_new, maxv);
+      return MPM_OK;
+    }
+  }
   const int ctas = BATCH ? di->fused_b_ctas[ep] : di->fused_ctas[ep][MODE];
   if (p.has_Ep)
     k_fused<true, MODE, BATCH><<<ctas, kP2GThreads, kFusedSmem, s>>>(p, tab, w, mx, mf, st, out, cap, n, dt,
@@ -2206,6 +2245,16 @@ int mpm_max_grid_velocity(const MpmParams *p, void *ws, int64_t cap, float *out,
   Ws w;
   ws_layout(*p, cap, (char *)ws, &w);
   k_max_grid_velocity<<<di->sms * 4, 256, 0, (cudaStream_t)stream>>>(*p, w, out);
+  return last_error();
+}
+
+int mpm_constitutive_eval(const MpmParams *p, int64_t n, const int32_t *material, float *F, const float *C,
+                          float *Jp, float *affine, float dt, void *stream) {
+  if (!params_ok(p) || p->n_scenes > 0 || n < 0 || (n > 0 && (!material || !F || !C || !Jp || !affine)))
+    return MPM_E_INVALID;
+  if (n == 0) return MPM_OK;
+  k_constitutive_eval<<<(unsigned)((n + 127) / 128), 128, 0, (cudaStream_t)stream>>>(*p, n, material, F, C, Jp,
+                                                                                      affine, dt);
   return last_error();
 }
 

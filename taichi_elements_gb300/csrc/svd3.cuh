@@ -107,8 +107,11 @@ __device__ __forceinline__ void cond_swap(bool doit, float (&B)[3][3], float (&V
 // det F > 0, where R equals U V^T of the SVD convention above.  Newton's
 // iteration converges quadratically: once a step moves R by at most 3e-4 the
 // remaining error is below about 5e-8, so the loop stops there.  Returns false
-// when that has not happened after MAX_ITERS steps (very large stretch); the
-// caller then uses the SVD.
+// when that has not happened after MAX_ITERS steps (very large stretch), and
+// for a nearly singular F (det F around 1e-17 relative to |F|^3, e.g. a
+// particle flattened against a wall), where the iterates overflow before they
+// converge; the caller then uses the SVD.  The iterates must stay finite:
+// fmaxf drops a NaN operand, so a NaN iterate would read as converged.
 template <int MAX_ITERS = 6>
 __device__ __forceinline__ bool polar_rotation(const float (&F)[3][3], float (&R)[3][3]) {
 #pragma unroll
@@ -129,6 +132,7 @@ __device__ __forceinline__ bool polar_rotation(const float (&F)[3][3], float (&R
     Cf[2][2] = R[0][0] * R[1][1] - R[0][1] * R[1][0];
     const float det = R[0][0] * Cf[0][0] + R[0][1] * Cf[0][1] + R[0][2] * Cf[0][2];
     const float h = 0.5f * rcp_nr(det);
+    if (!(fabsf(h) <= 3.0e38f)) return false;  // det overflowed, vanished or is NaN
     float change = 0.0f;
 #pragma unroll
     for (int i = 0; i < 3; ++i)
@@ -140,7 +144,12 @@ __device__ __forceinline__ bool polar_rotation(const float (&F)[3][3], float (&R
       }
     done = change <= 3e-4f;
   }
-  return done;
+  float sum = 0.0f;  // NaN or infinite if any entry is
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) sum += R[i][j];
+  return done && fabsf(sum) <= 3.0e38f;
 }
 
 template <int SWEEPS = 4>

@@ -168,8 +168,43 @@ def case_degenerate(rng):
     return dict(res=(24, 24, 24), state=s, postprocess=[], kw={}, no_trajectory=True)
 
 
+def case_flattened(rng):
+    """Particles flattened against the floor, the state a soft elastic cube
+    reaches some hundred substeps after it lands: the vertical row of F is
+    about 1e-9 times a combination of the other two rows (the small
+    off-diagonal rates of C make it so), so det F is at the level of float32
+    rounding, around 1e-17; C has a large negative vertical rate.  A layer
+    two cells above the floor of elastic, snow and stationary particles: the
+    materials whose rotation factor can come from Newton's polar iteration
+    instead of the SVD."""
+    n_each = 250
+    xs, ms = [], []
+    for k, m in enumerate([MAT_ELASTIC, MAT_SNOW, MAT_STATIONARY]):
+        cx = 0.3 + 0.2 * k
+        xs.append(np.column_stack([cx + 0.08 * (2 * rng.random(n_each) - 1),
+                                   (2.0 + 0.9 * rng.random(n_each)) / 24.0,
+                                   0.5 + 0.08 * (2 * rng.random(n_each) - 1)]))
+        ms.append(np.full(n_each, m, np.int32))
+    x = np.concatenate(xs).astype(np.float32)
+    mat = np.concatenate(ms)
+    n = len(x)
+    F = np.empty((n, 3, 3))
+    C = np.empty((n, 3, 3))
+    for p in range(n):
+        r0 = np.array([0.96 + 0.03 * rng.random(), 0.01 * rng.standard_normal(), 0.003 * rng.standard_normal()])
+        r2 = np.array([0.003 * rng.standard_normal(), 0.003 * rng.standard_normal(), 0.95 + 0.03 * rng.random()])
+        F[p] = [r0, 1e-9 * rng.standard_normal() * r0 + 1e-9 * rng.standard_normal() * r2, r2]
+        C[p] = 0.15 * rng.standard_normal((3, 3))
+        C[p, 1] = [1e-5 * rng.standard_normal(), -89.0 + rng.standard_normal(), 1e-5 * rng.standard_normal()]
+    v = (0.05 * rng.uniform(-1, 1, (n, 3))).astype(np.float32)
+    v[:, 1] = 0.0
+    s = dict(x=x, v=v, C=C.astype(np.float32), F=F.astype(np.float32), Jp=np.ones(n, np.float32), material=mat)
+    return dict(res=(24, 24, 24), state=s, postprocess=[], kw={}, no_trajectory=True)
+
+
 CASES = {"mixed_24": case_mixed, "walls_24": case_walls, "unbounded_24": case_unbounded,
-         "no_plasticity_24": case_no_plasticity, "degenerate_24": case_degenerate}
+         "no_plasticity_24": case_no_plasticity, "degenerate_24": case_degenerate,
+         "flattened_24": case_flattened}
 
 
 # ------------------------------------------------------------ running ----

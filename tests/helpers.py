@@ -103,7 +103,7 @@ def run_phases(solver, dt):
 
 # ------------------------------------------- reference-run fixtures ----
 
-REF_CASES = ["mixed_24", "walls_24", "unbounded_24", "no_plasticity_24", "degenerate_24"]
+REF_CASES = ["mixed_24", "walls_24", "unbounded_24", "no_plasticity_24", "degenerate_24", "flattened_24"]
 
 
 def ref_fixture(name):
@@ -142,12 +142,13 @@ def ref_config(g):
 
 
 def ref_particles(g, dtype=np.float64):
+    """The fixture's input state as oracle particles (copies: the oracle
+    updates them in place)."""
     n = int(g["n"])
     Jp = g["in_Jp"] if "in_Jp" in g else np.ones(n)
     C = g["in_C"] if "in_C" in g else np.zeros((n, 3, 3))
-    return O.Particles(np.ascontiguousarray(g["in_x"], dtype), np.ascontiguousarray(g["in_v"], dtype),
-                       np.ascontiguousarray(C, dtype), np.ascontiguousarray(g["in_F"], dtype),
-                       np.ascontiguousarray(Jp, dtype), np.ascontiguousarray(g["in_material"], np.int32))
+    return O.Particles(*(np.array(a, dtype) for a in (g["in_x"], g["in_v"], C, g["in_F"], Jp)),
+                       np.array(g["in_material"], np.int32))
 
 
 # -------------------------------------------------- tolerance table ----

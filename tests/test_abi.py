@@ -104,6 +104,8 @@ def test_argument_validation_without_gpu(lib):
     p.win_lo[0] = 3  # window origin must be block aligned
     assert L.mpm_workspace_bytes(ctypes.byref(p), 1024, ctypes.byref(size)) == -1
     assert L.mpm_gather_rows(None, 10, 5, 0, 3, None, None) == -1
+    assert L.mpm_constitutive_eval(ctypes.byref(p), 4, None, None, None, None, None, 1e-4, None) == -1
+    assert L.mpm_constitutive_eval(ctypes.byref(p), -1, None, None, None, None, None, 1e-4, None) == -1
 
 
 def test_solver_refuses_without_cuda():

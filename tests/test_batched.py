@@ -127,12 +127,13 @@ def test_batched_64_scenes_match_oracle():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("resort", [1, 3, 24])
-def test_batched_frames_match_per_substep_launches(resort):
+@pytest.mark.parametrize("resort,occupancy", [(1, 0), (3, 0), (24, 0), (3, 1), (24, 1)])
+def test_batched_frames_match_per_substep_launches(resort, occupancy):
     """mpm_batch_frame (fused frames, re-sorted about every `resort`
-    substeps) against the batch's per-substep launches: the same arithmetic
-    in another order, so positions agree to float32 rounding and every
-    scene's max |v| per substep matches."""
+    substeps; both register budgets of the fused kernel) against the batch's
+    per-substep launches: the same arithmetic in another order, so positions
+    agree to float32 rounding and every scene's max |v| per substep
+    matches."""
     from taichi_elements_gb300._lib import ROW_X
     from taichi_elements_gb300.batched import BatchedMPM
     bs = small_scenes()
@@ -140,6 +141,7 @@ def test_batched_frames_match_per_substep_launches(resort):
     b = BatchedMPM(bs, use_cuda_graph=False)
     a.fuse_frames = True
     a.resort_every = resort
+    a.occupancy = occupancy
     b.fuse_frames = False
     nsub = 10
     a.substeps(nsub)

@@ -29,15 +29,17 @@ magnitude; x and F on unit scale; v on the largest particle speed):
 Trajectories through step(frame_dt) (6 substeps): positions within rel L2
 1e-5 of the reference's float64 trajectory (the benchmark spec's 1e-3 is for 100
 substeps).  The fused mode is compared after each of three substeps with the
-plain bounds, except F and Jp at 2e-6: each substep multiplies them by a
-float32-rounded update, so their error grows by about 1e-6 per substep
-(measured 1.2e-6 after the second).
+plain bounds, except F and Jp at 2e-6 or 4x the float32 oracle's own error
+after that substep where larger: each substep multiplies them by a
+float32-rounded update, so their error grows by about 1e-6 per substep (the
+float32 oracle: 1.4e-6 for F and 2.2e-6 for Jp after the third).
 """
 import numpy as np
 import pytest
 import torch
 
-from helpers import REF_CASES, block_coords, ref_fixture, ref_kw, rel_inf, run_phases
+from helpers import REF_CASES, block_coords, ref_config, ref_fixture, ref_kw, ref_particles, rel_inf, run_phases
+from oracle import oracle as O
 from taichi_elements_gb300.mpm_solver import MPMSolver
 
 pytestmark = pytest.mark.gpu
@@ -157,16 +159,25 @@ def test_gpu_fused_mode_matches_reference_g2p2g():
     g = ref_fixture("g2p2g_24")
     s = make_solver(g, use_g2p2g=True)
     dt = float(g["substep_dt"])
+    # the float32 oracle's own F and Jp error after each substep calibrates
+    # their bound: 2e-6, or 4x that error where larger (it grows about 1e-6
+    # per substep; the oracle reaches 1.4e-6 and 2.2e-6 after the third)
+    cfg = ref_config(g)
+    P32 = ref_particles(g, np.float32)
+    R32 = O.G2P2GRunner(cfg, P32, O.Window.covering(np.asarray(g["in_x"], np.float64), cfg.inv_dx, margin=16))
     for k in range(3):
         s.step(dt)
+        R32.step(dt)
         st = s.full_state()
         vs = max(np.abs(g[f"sub{k}_v"]).max(), 1e-3)
         ex = rel_inf(st["x"].cpu().numpy(), g[f"sub{k}_x"], 1.0)
         ev = rel_inf(st["v"].cpu().numpy(), g[f"sub{k}_v"], vs)
         eF = rel_inf(st["F"].cpu().numpy(), g[f"sub{k}_F"], 1.0)
         eJ = rel_inf(st["Jp"].cpu().numpy(), g[f"sub{k}_Jp"], 1.0)
-        print(f"\ng2p2g substep {k}: x={ex:.2e} v={ev:.2e} F={eF:.2e} Jp={eJ:.2e}")
-        assert ex <= BOUND["x"] and ev <= BOUND["v"] and eF <= 2e-6 and eJ <= 2e-6
+        bF = max(2e-6, 4 * rel_inf(R32.P.F, g[f"sub{k}_F"], 1.0))
+        bJ = max(2e-6, 4 * rel_inf(R32.P.Jp, g[f"sub{k}_Jp"], 1.0))
+        print(f"\ng2p2g substep {k}: x={ex:.2e} v={ev:.2e} F={eF:.2e} (bound {bF:.1e}) Jp={eJ:.2e} (bound {bJ:.1e})")
+        assert ex <= BOUND["x"] and ev <= BOUND["v"] and eF <= bF and eJ <= bJ
 
 
 @pytest.mark.parametrize("name", REF_CASES)

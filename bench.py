@@ -692,16 +692,21 @@ def run_quant_measure(sc, substeps=50):
     return out
 
 
-def run_g2p2g_measure(sc, resort, substeps=50, warmup=5):
+def run_g2p2g_measure(sc, resort, substeps=50, warmup=5, tune=True):
     """The same scene in the fused G2P2G mode (MPMSolver(use_g2p2g=True),
     engine/mpm_solver.py:363-485): K substeps as one frame through
-    mpm_g2p2g_frame (what step() runs, re-sorted every `resort` substeps),
-    then K substeps of per-substep launches (substep() and the adaptive-dt
-    loop), each timed with CUDA events."""
+    mpm_g2p2g_frame (what step() runs, with the mode's own tuned re-sort
+    interval and register budget, or re-sorted every `resort` substeps
+    without the tuner), then K substeps of per-substep launches (substep()
+    and the adaptive-dt loop), each timed with CUDA events."""
     import torch
     s = sc.make_solver(use_g2p2g=True, chunk=512)
     s.use_cuda_graph = False
     s.resort_every = resort
+    tuned = None
+    if tune:
+        from taichi_elements_gb300.autotune import tune_schedule
+        tuned = tune_schedule(s)
     dt = sc.default_dt
     s._prepare(dt)
     s._maxv = torch.zeros(max(substeps, warmup), dtype=torch.float32, device=s.device)
@@ -716,6 +721,7 @@ def run_g2p2g_measure(sc, resort, substeps=50, warmup=5):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / substeps
 
+    s.fuse_frames = True  # the frames are measured whichever launch mode the tuner preferred
     s._launch_substeps(warmup, dt)  # the first frame: fresh particles, the mode's state
     evs, run = time_frames(s, dt, [substeps], stream)
     ms_frame = timed(run)
@@ -731,7 +737,9 @@ def run_g2p2g_measure(sc, resort, substeps=50, warmup=5):
     eff = s._frame_resort(substeps)
     sorts = (substeps + eff - 1) // eff
     out = {"value": n / (ms_frame / 1e3), "unit": "particle-substeps/s (fused G2P2G mode)",
-           "ms_per_substep": ms_frame, "substeps": substeps, "resort_every": resort,
+           "ms_per_substep": ms_frame, "substeps": substeps, "resort_every": s.resort_every,
+           "occupancy": s.occupancy,
+           "autotune": None if tuned is None else {k: tuned[k] for k in ("frame_ms", "frame_ms_rolled", "mode")},
            "gpu_launches": sorts * (FINALIZE_LAUNCHES + 4) + (sorts - 1) + (substeps - sorts) * 4 + 1,
            "ms_per_launch": {k: (sum(v) / len(v) if v else 0.0) for k, v in kt.items()},
            "per_substep_launches": {"value": n / (ms_sub / 1e3), "ms_per_substep": ms_sub},

@@ -153,9 +153,9 @@ def ref_particles(g, dtype=np.float64):
 
 # -------------------------------------------------- tolerance table ----
 # Relative L-inf bounds of one GPU substep against float64 (the oracle or
-# the reference's own run).  Spec bounds: grid m / mv 1e-5, particle
+# the reference's own run).  Target bounds: grid m / mv 1e-5, particle
 # x / F 1e-6 (Jp on F's scale).  Calibrated (the reference's own float32 run
-# is farther than the benchmark spec's 1e-6 from its float64 run, see
+# is farther than the target 1e-6 from its float64 run, see
 # tests/test_gpu_reference_golden.py): v 1e-5, grid v 1e-5, C 2e-5.
 BOUND = {"grid_m": 1e-5, "grid_mv": 1e-5, "grid_v": 1e-5, "x": 1e-6, "F": 1e-6, "Jp": 1e-6, "v": 1e-5, "C": 2e-5}
 

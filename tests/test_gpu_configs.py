@@ -1,7 +1,7 @@
 """Parity at the benchmark configurations themselves, at full size.
 
 * The 134,218-particle water cube on a 64^3 grid over 100 substeps:
-  positions within rel L2 1e-3 of the float64 oracle (the benchmark spec's
+  positions within rel L2 1e-3 of the float64 oracle (the target
   trajectory bound), and the per-substep max |v| of compute_max_velocity.
 * The 2M-particle four-material scene (128^3) and the 16M-particle
   ellipsoid scene (256^3): one substep from an evolved state, phase by phase

@@ -13,21 +13,21 @@ magnitude; x and F on unit scale; v on the largest particle speed):
 
   field    bound   source
   binning  exact   active blocks, per-block counts, grid-active blocks
-  grid_m   1e-5    north star (grid mass)
-  grid_mv  1e-5    north star (grid momentum)
-  x        1e-6    north star
-  F        1e-6    north star
+  grid_m   1e-5    target (grid mass)
+  grid_mv  1e-5    target (grid momentum)
+  x        1e-6    target
+  F        1e-6    target
   Jp       1e-6    same scale as F
   v        1e-5    calibrated: the reference's own float32 run is 0.5-2.8e-6
                    from its float64 run on these states (reordered float32
-                   sums of 27 nodes), above the benchmark spec's 1e-6
+                   sums of 27 nodes), above the target 1e-6
   grid_v   1e-5    calibrated: v = mv / m divides two 1e-6-accurate sums;
                    the reference's float32 run reaches 5.7e-6
   C        2e-5    calibrated: C sums 27 terms of |w v dpos| * 4 inv_dx; the
                    reference's float32 run reaches 3.1e-6
 
 Trajectories through step(frame_dt) (6 substeps): positions within rel L2
-1e-5 of the reference's float64 trajectory (the benchmark spec's 1e-3 is for 100
+1e-5 of the reference's float64 trajectory (the target 1e-3 is for 100
 substeps).  The fused mode is compared after each of three substeps with the
 plain bounds, except F and Jp at 2e-6 or 4x the float32 oracle's own error
 after that substep where larger: each substep multiplies them by a

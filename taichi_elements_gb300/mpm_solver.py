@@ -1050,9 +1050,10 @@ class MPMSolver:
         """engine/mpm_solver.py:1172-1191: copies in original particle order.
 
         The arrays are gathered on the device and copied into page-locked
-        host memory (PyTorch's caching host allocator, so repeated frames
-        reuse it) with one synchronisation for all of them; each returned
-        numpy array owns its buffer like the reference's fresh copies."""
+        host buffers with one synchronisation for all of them.  The buffers
+        come from a process-wide pool (_pinned_buffer) and are handed out
+        again only once nothing references the returned arrays (or a view of
+        them), so a caller can keep them as the reference's fresh copies."""
         n = self.n_particles
         if n == 0:
             data = {'position': np.zeros((0, 3), np.float32), 'velocity': np.zeros((0, 3), np.float32),

@@ -76,7 +76,8 @@ def test_batched_64_scenes_match_oracle():
     """The 64-scene batch of the batched benchmark (grids 32-96^3, 8K-300K
     particles in 1-3 cubes, four materials, per-scene E from 1e4 to 1e6),
     with a collider per scene and initial velocities added, 8 substeps in
-    one batched frame; every scene against the float64 oracle run with that
+    one batched frame, launched per substep and as fused frames; every scene
+    against the float64 oracle run with that
     scene's own constants, dt and colliders.  Positions on unit scale and
     velocities on the scene's largest speed, relative L-inf, with the bound
     table of tests/helpers.py raised to 4x the float32 oracle's own error
@@ -97,16 +98,22 @@ def test_batched_64_scenes_match_oracle():
         else:
             pp = [dict(kind=0, surface=1, point=(0.5, 0.2, 0.5), normal=(0.0, 1.0, 0.0), friction=0.0)]
         bs.append(BatchScene(sc.res, sc.x, sc.material, v, E_scale=sc.E_scale, postprocess=pp))
-    B = BatchedMPM(bs, use_cuda_graph=False)
     nsub = 8
-    B.substeps(nsub)
-    B.check_status()
-    worst = {"x": (0.0, 0.0), "v": (0.0, 0.0)}
-    threads = os.cpu_count() or 1
     from taichi_elements_gb300._lib import ROW_V, ROW_X
-    X = B._gather(ROW_X, 3).cpu().numpy()
-    V = B._gather(ROW_V, 3).cpu().numpy()
-    off = [int(o) for o in B.offsets]
+    # per-substep launches (the default), and fused frames (mpm_batch_frame,
+    # re-sorted every 3 substeps, the 16-warp fused kernel)
+    runs_gpu = {}
+    for label, fuse in (("per-substep", False), ("fused frames", True)):
+        B = BatchedMPM(bs, use_cuda_graph=False)
+        if fuse:
+            B.fuse_frames, B.resort_every, B.occupancy = True, 3, 1
+        B.substeps(nsub)
+        B.check_status()
+        runs_gpu[label] = (B._gather(ROW_X, 3).cpu().numpy(), B._gather(ROW_V, 3).cpu().numpy(),
+                           [int(o) for o in B.offsets])
+        del B
+    worst = {label: {"x": (0.0, 0.0), "v": (0.0, 0.0)} for label in runs_gpu}
+    threads = os.cpu_count() or 1
     for i, s in enumerate(bs):
         cfg = O.Config(res=s.res, E_scale=s.E / 1e6, gravity=s.gravity, postprocess=s.postprocess)
         runs = {}
@@ -116,14 +123,17 @@ def test_batched_64_scenes_match_oracle():
             runs[dtype] = R.P
         P64, P32 = runs[np.float64], runs[np.float32]
         vs = max(np.abs(P64.v).max(), 1e-3)
-        errs = {"x": (rel_inf(X[off[i]:off[i + 1]], P64.x, 1.0), rel_inf(P32.x, P64.x, 1.0)),
-                "v": (rel_inf(V[off[i]:off[i + 1]], P64.v, vs), rel_inf(P32.v, P64.v, vs))}
-        assert_bounds(f"scene {i} ({s.n} particles, {s.res[0]}^3, E {s.E:.3g})", errs, f32_calibrated=True)
-        for k in worst:
-            if errs[k][0] > worst[k][0]:
-                worst[k] = errs[k]
-    print(f"\nworst over {len(bs)} scenes: x {worst['x'][0]:.2e} (f32 {worst['x'][1]:.1e}), "
-          f"v {worst['v'][0]:.2e} (f32 {worst['v'][1]:.1e})")
+        for label, (X, V, off) in runs_gpu.items():
+            errs = {"x": (rel_inf(X[off[i]:off[i + 1]], P64.x, 1.0), rel_inf(P32.x, P64.x, 1.0)),
+                    "v": (rel_inf(V[off[i]:off[i + 1]], P64.v, vs), rel_inf(P32.v, P64.v, vs))}
+            assert_bounds(f"{label}, scene {i} ({s.n} particles, {s.res[0]}^3, E {s.E:.3g})", errs,
+                          f32_calibrated=True)
+            for k in worst[label]:
+                if errs[k][0] > worst[label][k][0]:
+                    worst[label][k] = errs[k]
+    for label, w in worst.items():
+        print(f"\n{label}: worst over {len(bs)} scenes: x {w['x'][0]:.2e} (f32 {w['x'][1]:.1e}), "
+              f"v {w['v'][0]:.2e} (f32 {w['v'][1]:.1e})")
 
 
 @pytest.mark.gpu

@@ -270,6 +270,7 @@ class MPMSolver:
         # device reduction after a frame's readback; None when unknown
         self._host_box = None
         self._readback = None  # page-locked buffers of the end-of-frame readback
+        self._copy_stream = None  # side stream of particle_info's host copies
         self._set_window(*self._box_window())
 
     # ---------------------------------------------------------- params ---
@@ -515,7 +516,10 @@ class MPMSolver:
         assert self.n_particles + n <= self.max_num_particles
         self._ensure_capacity(n)
         a, b = self.n_particles, self.n_particles + n
-        s = torch.empty((NROWS, n), dtype=torch.float32, device=self.device)
+        st = self._state[self._cur]
+        # float32 storage: the rows are written in place (slots a..b of the
+        # state); packed storage builds them in float32 and packs them below
+        s = torch.empty((NROWS, n), dtype=torch.float32, device=self.device) if self.quant else st[:, a:b]
         si = s.view(torch.int32)
         s[ROW_X:ROW_X + 3] = x.t()
         if isinstance(velocity, torch.Tensor):
@@ -551,13 +555,10 @@ class MPMSolver:
             s[ROW_F:ROW_F + 9] = F.reshape(n, 9).t().to(self.device, torch.float32)
         if Jp is not None:
             s[ROW_JP] = Jp.to(self.device, torch.float32)
-        st = self._state[self._cur]
         if self.quant:
             _lib.check(
                 self._lib.mpm_quant_pack(_ptr(s), n, n, _ptr(st), self._cap, a, None, self.stream),
                 "mpm_quant_pack")
-        else:
-            st[:, a:b] = s
         if isinstance(color, torch.Tensor):
             self._color[a:b] = color.to(self.device, torch.int32)
         else:
@@ -1061,16 +1062,36 @@ class MPMSolver:
             if self.use_emitter_id:
                 data['emitter_ids'] = np.zeros(0, np.int32)
             return data
-        rows = self._rows_f32()
-        dev = {
-            'position': self._gather(ROW_X, 3, rows),
-            'velocity': self._gather(ROW_V, 3, rows),
-            'material': self._gather(ROW_MAT, 1, rows).view(torch.int32).reshape(n) & 0xFF,
-            'color': self._color[:n],
-        }
+        # the copies run on a side stream, each behind its own gather, so the
+        # copy engine works while the next field is gathered; the resident
+        # fields go first
+        main = torch.cuda.current_stream(self.device)
+        if self._copy_stream is None:
+            self._copy_stream = torch.cuda.Stream(device=self.device)
+        side = self._copy_stream
+        side.wait_stream(main)
+        host = {}
+
+        def copy(name, t):
+            h, hn = _pinned_buffer(t.shape, t.dtype)
+            t.record_stream(side)
+            with torch.cuda.stream(side):
+                h.copy_(t, non_blocking=True)
+            host[name] = hn
+
+        copy('color', self._color[:n])
         if self.use_emitter_id:
-            dev['emitter_ids'] = self._emitter[:n]
-        return dict(zip(dev.keys(), self._to_host(*dev.values())))
+            copy('emitter_ids', self._emitter[:n])
+        rows = self._rows_f32()
+        for name, gather in (('position', lambda: self._gather(ROW_X, 3, rows)),
+                             ('velocity', lambda: self._gather(ROW_V, 3, rows)),
+                             ('material', lambda: self._gather(ROW_MAT, 1, rows).view(torch.int32).reshape(n) & 0xFF)):
+            t = gather()
+            side.wait_stream(main)
+            copy(name, t)
+        side.synchronize()
+        keys = ['position', 'velocity', 'material', 'color'] + (['emitter_ids'] if self.use_emitter_id else [])
+        return {k: host[k] for k in keys}
 
     def _to_host(self, *tensors):
         """numpy copies of device tensors through page-locked buffers, one

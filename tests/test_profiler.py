@@ -4,7 +4,8 @@ prints Taichi's kernel and memory profiler tables there).
 CPU: the decoding of a frame's events into launch groups, for plain and
 G2P2G frames, and the table.  GPU: step(print_stat=True) with the profiler on
 prints every launch group of the frame with the counts its schedule implies,
-the memory table, and leaves the simulation's result unchanged.
+the memory table, and leaves the simulation's result unchanged; batched
+frames are recorded too.
 """
 import contextlib
 import io
@@ -140,3 +141,29 @@ def test_print_stat_prints_launch_groups(use_g2p2g):
     a = s0.particle_info()["position"].astype(np.float64)
     b = s1.particle_info()["position"].astype(np.float64)
     assert np.abs(a - b).max() <= 1e-5
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fuse", [False, True])
+def test_batched_frames_are_profiled(fuse):
+    import torch
+
+    from test_batched import small_scenes
+    from taichi_elements_gb300.batched import BatchedMPM
+    profiler.enable()
+    profiler.clear_kernel_profiler_info()
+    B = BatchedMPM(small_scenes())
+    B.fuse_frames, B.resort_every = fuse, 4
+    for _ in range(2):  # the second frame would replay a graph without the profiler
+        B.substeps(10)
+    B.check_status()
+    torch.cuda.synchronize()
+    rows = {name: cnt for name, cnt, *_ in profiler.kernel_profiler_table()}
+    if fuse:
+        from taichi_elements_gb300.mpm_solver import frame_resort_interval
+        r = frame_resort_interval(10, 4)
+        sorts = 2 * ((10 + r - 1) // r)
+        assert rows["batch k_p2g"] == sorts and rows["batch k_fused"] == 20 - sorts
+        assert rows["batch grid"] == 20 and rows["batch k_g2p_stream"] == sorts
+    else:
+        assert rows == {"mpm_batch_substep": 20}

@@ -972,6 +972,21 @@ class MPMSolver:
         rows.append(("max |v| per substep", self._maxv.numel() * 4))
         return rows
 
+    def compute_max_velocity(self) -> float:
+        """engine/mpm_solver.py:726-735: the largest velocity component
+        magnitude max_p max_d |v_pd| over the particles (0 without any)."""
+        n = self.n_particles
+        if n == 0:
+            return 0.0
+        return float(self._rows_f32()[ROW_V:ROW_V + 3, :n].abs().max().item())
+
+    def compute_max_grid_velocity(self, grid_v=None) -> float:
+        """engine/mpm_solver.py:737-746: the largest velocity component
+        magnitude over the grid nodes of the last substep (0 before the
+        first).  `grid_v` names the reference's grid field; the engine has
+        one grid, so the argument is accepted and not used."""
+        return self._max_grid_velocity()
+
     def _max_grid_velocity(self) -> float:
         """compute_max_grid_velocity (engine/mpm_solver.py:737-746) of the
         last substep's grid (0 before the first)."""

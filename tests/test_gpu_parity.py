@@ -13,8 +13,8 @@ import numpy as np
 import pytest
 import torch
 
-from helpers import (assert_bounds, block_coords, lib_call, oracle_config, particles_from_solver, rel_inf,
-                     run_phases, window_lookup)
+from helpers import (assert_bounds, block_coords, gpu_grid, lib_call, oracle_config, particles_from_solver,
+                     rel_inf, run_phases, window_lookup)
 from oracle import oracle as O
 from taichi_elements_gb300 import scenes
 from taichi_elements_gb300.mpm_solver import MPMSolver, MPMError
@@ -399,3 +399,18 @@ def test_sticky_sphere_and_slip_plane_trajectory():
         s.substep(dt)
     g = s.full_state()['x'].cpu().numpy().astype(np.float64)
     assert np.linalg.norm(g - R.P.x) / np.linalg.norm(R.P.x) < 1e-3
+
+
+def test_max_velocity_queries():
+    """compute_max_velocity (engine/mpm_solver.py:726-735) on the particles'
+    velocities and compute_max_grid_velocity (:737-746) on the last
+    substep's grid, against numpy on the same data."""
+    sc = scenes.smoke_scene()
+    s = sc.make_solver()
+    assert s.compute_max_velocity() == pytest.approx(float(np.abs(sc.v).max()), rel=1e-7)
+    assert s.compute_max_grid_velocity() == 0.0
+    s.step(6 * sc.default_dt)
+    v = s.particle_info()["velocity"]
+    assert s.compute_max_velocity() == float(np.abs(v).max())
+    _, vel = gpu_grid(s.views(), "grid_vel")
+    assert s.compute_max_grid_velocity(None) == pytest.approx(float(np.abs(vel[:, :3]).max()), rel=1e-7)

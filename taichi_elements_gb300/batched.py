@@ -241,7 +241,7 @@ class BatchedMPM:
         """All `count` substeps as one fused frame (mpm_batch_frame)."""
         in_b = ctypes.c_int32(0)
         resort = frame_resort_interval(count, self.resort_every)
-        evs, arr = profiler.frame_events(count) if profiler.kernel_profiler else (None, None)
+        evs, arr = profiler.frame_events(count, self.device) if profiler.kernel_profiler else (None, None)
         _lib.check(self._lib.mpm_batch_frame(ctypes.byref(self._header), self._rows.data_ptr(), self._ws.data_ptr(),
                                              self.cap, self.n_particles, self._state[self._cur].data_ptr(),
                                              self._state[1 - self._cur].data_ptr(), int(count),

@@ -835,7 +835,7 @@ class MPMSolver:
         the G2P2G mode's substeps."""
         p = self.params
         in_b = ctypes.c_int32(0)
-        evs, arr = profiler.frame_events(count) if profiler.kernel_profiler else (None, None)
+        evs, arr = profiler.frame_events(count, self.device) if profiler.kernel_profiler else (None, None)
         if self.use_g2p2g:
             if self._g2p2g_listed:  # per-substep calls left finalized lists: count afresh
                 _lib.check(self._lib.mpm_bin_count(ctypes.byref(p), _ptr(self._ws), self._cap,

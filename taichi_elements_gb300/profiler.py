@@ -36,17 +36,20 @@ def clear_kernel_profiler_info() -> None:
     _pending.clear()
 
 
-def frame_events(count: int):
+def frame_events(count: int, device=None):
     """Timing events for one frame of `count` substeps and the ctypes array
     of their handles, in the order the frame records them: events[5k + j]
     for substep k (its start; after the binning of the state, i.e. the
     previous plain run's closing G2P or the G2P2G mode's binning pass; after
     the sort's finalize; after the particle kernel; after the grid update),
-    events[5 count] and [5 count + 1] around the frame's closing pass."""
+    events[5 count] and [5 count + 1] around the frame's closing pass.
+    The events belong to `device` (the current one by default) and are
+    created on its current stream, the one the frame launches on."""
     evs = [torch.cuda.Event(enable_timing=True) for _ in range(5 * count + 2)]
-    stream = torch.cuda.current_stream()
-    for e in evs:
-        e.record(stream)  # creates the event before its handle is taken
+    with torch.cuda.device(device):
+        stream = torch.cuda.current_stream()
+        for e in evs:
+            e.record(stream)  # creates the event before its handle is taken
     return evs, (ctypes.c_void_p * len(evs))(*[e.cuda_event for e in evs])
 
 

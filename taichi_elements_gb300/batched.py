@@ -273,7 +273,7 @@ class BatchedMPM:
         elif self.use_cuda_graph and g is None and key in self._seen:
             start = self._cur
             g = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(g):
+            with torch.cuda.graph(g, capture_error_mode="thread_local"):  # other threads keep their solvers running
                 self._launch_all(count)
             self._cur = start
             self._graphs[key] = g

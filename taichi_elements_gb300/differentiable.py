@@ -136,7 +136,7 @@ class Rollout:
         g = self._graphs.get(key)
         if g is None and self.use_cuda_graph and key in self._seen:
             g = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(g):
+            with torch.cuda.graph(g, capture_error_mode="thread_local"):  # other threads keep their solvers running
                 fn(count)
             self._graphs[key] = g
         if g is not None:

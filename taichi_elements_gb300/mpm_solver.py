@@ -896,7 +896,7 @@ class MPMSolver:
         if g is None and key in self._graph_seen:
             start_cur = self._cur
             g = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(g):
+            with torch.cuda.graph(g, capture_error_mode="thread_local"):  # other threads keep their solvers running
                 self._launch_substeps(count, dt)
             self._cur = start_cur  # capture does not execute
             self._graphs[key] = g

@@ -119,7 +119,7 @@ def time_chunks(solver, candidates=CANDIDATES, substeps=8, dt=None):
         e0.record(stream)
         run(substeps)
         e1.record(stream)
-        torch.cuda.synchronize()
+        e1.synchronize()
         out[int(c)] = e0.elapsed_time(e1) / substeps
     return out
 
@@ -190,7 +190,7 @@ def time_frames(solver, candidates=RESORT_CANDIDATES, substeps=48, dt=None, occu
         e0.record(stream)
         frame()
         e1.record(stream)
-        torch.cuda.synchronize()
+        e1.synchronize()
         out[int(r)] = e0.elapsed_time(e1) / substeps
     return out
 

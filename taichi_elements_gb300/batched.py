@@ -19,7 +19,7 @@ import numpy as np
 import torch
 
 from . import _lib, profiler
-from .mpm_solver import frame_resort_interval
+from .mpm_solver import capture_graph, frame_resort_interval
 from ._lib import KIND_BOX, KIND_SURFACE, NROWS, ROW_C, ROW_F, ROW_ID, ROW_JP, ROW_MAT, ROW_V, ROW_X
 
 MARGIN = 8  # grid nodes kept around each scene's domain
@@ -272,9 +272,7 @@ class BatchedMPM:
             g = None
         elif self.use_cuda_graph and g is None and key in self._seen:
             start = self._cur
-            g = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(g, capture_error_mode="thread_local"):  # other threads keep their solvers running
-                self._launch_all(count)
+            g = capture_graph(self.device, lambda: self._launch_all(count))
             self._cur = start
             self._graphs[key] = g
         if g is not None:

@@ -25,7 +25,7 @@ import torch
 
 from . import _lib
 from ._lib import NROWS, ROW_C, ROW_EP, ROW_F, ROW_ID, ROW_V, ROW_X
-from .mpm_solver import MPMSolver
+from .mpm_solver import MPMSolver, capture_graph
 
 GROWS = 26  # dL/dx 3, dL/dv 3, dL/dC 9, dL/dF 9, dL/dJp 1, dL/dE 1
 GROW_V, GROW_E = 3, 25
@@ -135,9 +135,7 @@ class Rollout:
         key = (kind, count)
         g = self._graphs.get(key)
         if g is None and self.use_cuda_graph and key in self._seen:
-            g = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(g, capture_error_mode="thread_local"):  # other threads keep their solvers running
-                fn(count)
+            g = capture_graph(self.dev, lambda: fn(count))
             self._graphs[key] = g
         if g is not None:
             g.replay()
@@ -266,7 +264,7 @@ class Rollout:
             if keep_checkpoints:
                 self.ckpt[seg].copy_(self.a)
             self._graphed("fwd", self._seg_len(seg), self._forward_ops)
-        torch.cuda.synchronize()
+        torch.cuda.current_stream(self.dev).synchronize()
         self._check()
         return self.by_id(self.a, ROW_X, 3)
 
@@ -286,7 +284,7 @@ class Rollout:
             (self.ring[0] if self.keep_workspaces else self.a).copy_(self.ckpt[seg])
             self._graphed("rec", count, self._recompute_ops)
             self._graphed("adj", count, self._adjoint_ops)
-        torch.cuda.synchronize()
+        torch.cuda.current_stream(self.dev).synchronize()
         extra = 0
         if self.keep_workspaces:
             off = self._status_off

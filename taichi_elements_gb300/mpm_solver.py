@@ -107,6 +107,26 @@ def _pinned_buffer_locked(shape, dtype):
     return pair
 
 
+def capture_graph(device, launch) -> torch.cuda.CUDAGraph:
+    """A CUDA graph of the launches `launch()` makes, captured on a side
+    stream ordered after the current one.  Unlike torch.cuda.graph this makes
+    no device-wide synchronisation and frees no cached memory, and the
+    capture restricts only the capturing thread, so solvers driven from other
+    host threads keep launching, copying and capturing meanwhile."""
+    g = torch.cuda.CUDAGraph()
+    main = torch.cuda.current_stream(device)
+    side = torch.cuda.Stream(device=device)
+    side.wait_stream(main)
+    with torch.cuda.stream(side):
+        g.capture_begin(capture_error_mode="thread_local")
+        try:
+            launch()
+        finally:
+            g.capture_end()
+    main.wait_stream(side)
+    return g
+
+
 def frame_resort_interval(count: int, target: int) -> int:
     """Re-sort interval for a fused frame of `count` substeps and a target
     interval: round(count / target) sorts (at least one) at equal spacing,
@@ -895,9 +915,7 @@ class MPMSolver:
         g = self._graphs.get(key)
         if g is None and key in self._graph_seen:
             start_cur = self._cur
-            g = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(g, capture_error_mode="thread_local"):  # other threads keep their solvers running
-                self._launch_substeps(count, dt)
+            g = capture_graph(self.device, lambda: self._launch_substeps(count, dt))
             self._cur = start_cur  # capture does not execute
             self._graphs[key] = g
         if g is not None:

@@ -22,7 +22,7 @@ kernel_profiler = False
 
 # launch group -> durations (ms)
 _records: dict[str, list[float]] = {}
-# (decode, name prefix) of the calls whose events have not been read yet
+# (decode, name prefix, last event) of the calls whose events have not been read yet
 _pending: list = []
 
 
@@ -82,7 +82,7 @@ def frame_kernel_times(count: int, evs, resort: int, g2p2g: bool = False) -> dic
 
 def add_frame(count: int, evs, resort: int, g2p2g: bool = False, prefix: str = "") -> None:
     """Queue a frame's events for the records."""
-    _pending.append((lambda: frame_kernel_times(count, evs, resort, g2p2g), prefix))
+    _pending.append((lambda: frame_kernel_times(count, evs, resort, g2p2g), prefix, evs[-1]))
 
 
 def substep_events():
@@ -92,17 +92,18 @@ def substep_events():
 
 def add_call(name: str, e0, e1) -> None:
     """Queue one timed call (both events recorded)."""
-    _pending.append((lambda: {name: [e0.elapsed_time(e1)]}, ""))
+    _pending.append((lambda: {name: [e0.elapsed_time(e1)]}, "", e1))
 
 
 def collect(sync: bool = True) -> None:
-    """Move the queued event durations into the records (synchronising the
-    device first unless the caller already has)."""
+    """Move the queued event durations into the records (waiting for each
+    call's last event first unless the caller already synchronised)."""
     if not _pending:
         return
     if sync:
-        torch.cuda.synchronize()
-    for decode, prefix in _pending:
+        for _, _, last in _pending:
+            last.synchronize()
+    for decode, prefix, _ in _pending:
         for name, ms in decode().items():
             if ms:
                 _records.setdefault(prefix + name, []).extend(ms)

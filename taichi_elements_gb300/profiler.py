@@ -15,6 +15,7 @@ synchronisation, so profiling adds no host round trip to a frame.
 from __future__ import annotations
 
 import ctypes
+import threading
 
 import torch
 
@@ -24,6 +25,8 @@ kernel_profiler = False
 _records: dict[str, list[float]] = {}
 # (decode, name prefix, last event) of the calls whose events have not been read yet
 _pending: list = []
+# solvers in several host threads share the records
+_lock = threading.Lock()
 
 
 def enable(on: bool = True) -> None:
@@ -32,8 +35,9 @@ def enable(on: bool = True) -> None:
 
 
 def clear_kernel_profiler_info() -> None:
-    _records.clear()
-    _pending.clear()
+    with _lock:
+        _records.clear()
+        _pending.clear()
 
 
 def frame_events(count: int, device=None):
@@ -82,7 +86,8 @@ def frame_kernel_times(count: int, evs, resort: int, g2p2g: bool = False) -> dic
 
 def add_frame(count: int, evs, resort: int, g2p2g: bool = False, prefix: str = "") -> None:
     """Queue a frame's events for the records."""
-    _pending.append((lambda: frame_kernel_times(count, evs, resort, g2p2g), prefix, evs[-1]))
+    with _lock:
+        _pending.append((lambda: frame_kernel_times(count, evs, resort, g2p2g), prefix, evs[-1]))
 
 
 def substep_events():
@@ -92,28 +97,40 @@ def substep_events():
 
 def add_call(name: str, e0, e1) -> None:
     """Queue one timed call (both events recorded)."""
-    _pending.append((lambda: {name: [e0.elapsed_time(e1)]}, "", e1))
+    with _lock:
+        _pending.append((lambda: {name: [e0.elapsed_time(e1)]}, "", e1))
 
 
 def collect(sync: bool = True) -> None:
-    """Move the queued event durations into the records (waiting for each
-    call's last event first unless the caller already synchronised)."""
-    if not _pending:
-        return
-    if sync:
-        for _, _, last in _pending:
-            last.synchronize()
-    for decode, prefix, _ in _pending:
-        for name, ms in decode().items():
-            if ms:
-                _records.setdefault(prefix + name, []).extend(ms)
-    _pending.clear()
+    """Move the queued event durations into the records: every queued call,
+    waiting for its last event (sync), or only the calls whose last event has
+    completed (a solver's own frame after its readback; calls of solvers in
+    other threads may still be running and stay queued)."""
+    with _lock:
+        pending = list(_pending)
+        _pending.clear()
+    done, keep = [], []
+    for item in pending:
+        if sync:
+            item[2].synchronize()
+        elif not item[2].query():
+            keep.append(item)
+            continue
+        done.append(item)
+    results = [(prefix, decode()) for decode, prefix, _ in done]
+    with _lock:
+        _pending.extend(keep)
+        for prefix, r in results:
+            for name, ms in r.items():
+                if ms:
+                    _records.setdefault(prefix + name, []).extend(ms)
 
 
 def query_kernel_profiler_info(name: str) -> dict:
     """count, total, min, avg and max (ms) of one launch group."""
     collect()
-    ms = _records.get(name, [])
+    with _lock:
+        ms = list(_records.get(name, []))
     if not ms:
         return {"count": 0, "total_ms": 0.0, "min_ms": 0.0, "avg_ms": 0.0, "max_ms": 0.0}
     return {"count": len(ms), "total_ms": sum(ms), "min_ms": min(ms), "avg_ms": sum(ms) / len(ms),
@@ -124,7 +141,9 @@ def kernel_profiler_table() -> list:
     """(name, count, total ms, min, avg, max) per launch group, largest total first."""
     collect()
     rows = []
-    for name, ms in _records.items():
+    with _lock:
+        items = [(name, list(ms)) for name, ms in _records.items()]
+    for name, ms in items:
         rows.append((name, len(ms), sum(ms), min(ms), sum(ms) / len(ms), max(ms)))
     rows.sort(key=lambda r: -r[2])
     return rows

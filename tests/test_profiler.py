@@ -26,6 +26,12 @@ class _Ev:
     def elapsed_time(self, other):
         return other.t - self.t
 
+    def query(self):
+        return True
+
+    def synchronize(self):
+        pass
+
 
 def _events(count):
     # event i recorded at time i^2 / 8: every interval distinct
@@ -88,6 +94,30 @@ def test_records_table_and_print():
     assert "100.00%" in text
     profiler.clear_kernel_profiler_info()
     assert profiler.kernel_profiler_table() == []
+
+
+def test_collect_keeps_unfinished_calls():
+    """Without a wait, calls whose last event has not completed (a solver in
+    another thread still running) stay queued until they have."""
+    profiler.enable()
+
+    class Pending(_Ev):
+        done = False
+
+        def query(self):
+            return self.done
+
+    late = Pending(2.0)
+    profiler.add_call("a", _Ev(0.0), _Ev(1.0))
+    profiler.add_call("b", _Ev(0.0), late)
+    profiler.collect(sync=False)
+    assert len(profiler._pending) == 1 and list(profiler._records) == ["a"]
+    profiler.collect(sync=False)
+    assert len(profiler._pending) == 1
+    late.done = True
+    profiler.collect(sync=False)
+    assert not profiler._pending
+    assert profiler.query_kernel_profiler_info("b")["total_ms"] == 2.0
 
 
 def test_off_prints_a_hint():
